@@ -1,0 +1,13 @@
+"""GB300-native voxelization engine: a drop-in for the voxelize / voxelize_solid path of
+Forceflow/cuda_voxelizer, implemented as hand-written sm_103a CUDA behind a C ABI (include/cvx.h).
+
+The native library ``_lib/libcvx.so`` is required; importing this package without it raises
+ImportError.
+"""
+from .api import (CvxError, Job, Plan, VoxInfo, create_mesh_bbox_cube, device_status, get_tuning, make_info,
+                  make_voxinfo, mesh_bbox, set_tuning, table_words, voxelize, voxelize_batch, voxelize_host,
+                  voxelize_solid, voxelize_ws, workspace_size)
+
+__all__ = ["CvxError", "Job", "Plan", "VoxInfo", "create_mesh_bbox_cube", "device_status", "get_tuning",
+           "make_info", "make_voxinfo", "mesh_bbox", "set_tuning", "table_words", "voxelize", "voxelize_batch",
+           "voxelize_host", "voxelize_solid", "voxelize_ws", "workspace_size"]

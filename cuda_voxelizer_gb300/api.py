@@ -1,0 +1,212 @@
+"""Python mirror of the reference's voxelization interface, on top of the C ABI.
+
+Names and argument meaning follow the reference: ``voxelize(info, triangle_data, vtable,
+morton_code)`` and ``voxelize_solid(...)`` (src/voxelize.cu:192, src/voxelize_solid.cu:147), a
+``voxinfo`` with bbox / gridsize / n_triangles / unit (src/util.h:50-69), ``createMeshBBCube``
+(src/util.h:80-110).  Device buffers are torch CUDA tensors or raw device pointers (int); PyTorch
+is only used for device memory and streams.  Errors raise :class:`CvxError` (the reference exits the
+process instead).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Sequence
+
+import numpy as np
+
+from ._lib import CvxError, CvxJob, CvxTuning, CvxVoxinfo, check, lib
+
+__all__ = ["VoxInfo", "voxelize", "voxelize_solid", "voxelize_ws", "workspace_size", "create_mesh_bbox_cube",
+           "mesh_bbox", "make_voxinfo", "table_words", "Job", "voxelize_batch", "Plan", "device_status",
+           "get_tuning", "set_tuning", "CvxError", "voxelize_host"]
+
+
+VoxInfo = CvxVoxinfo
+
+
+def _vec3(a) -> ctypes.Array:
+    a = np.asarray(a, dtype=np.float32).reshape(3)
+    return (ctypes.c_float * 3)(*[float(x) for x in a])
+
+
+def make_info(bbox_min, bbox_max, gridsize, n_triangles: int) -> VoxInfo:
+    """voxinfo constructor (src/util.h:56-61): unit = (max - min) / float(gridsize)."""
+    if np.isscalar(gridsize):
+        gridsize = (gridsize, gridsize, gridsize)
+    g = (ctypes.c_uint32 * 3)(*[int(x) for x in gridsize])
+    info = VoxInfo()
+    check(lib.cvx_voxinfo_init(ctypes.byref(info), _vec3(bbox_min), _vec3(bbox_max), g, int(n_triangles)),
+          "cvx_voxinfo_init")
+    return info
+
+
+def create_mesh_bbox_cube(bbox_min, bbox_max):
+    """createMeshBBCube (src/util.h:80-110) on float32 bounds."""
+    lo = (ctypes.c_float * 3)()
+    hi = (ctypes.c_float * 3)()
+    check(lib.cvx_bbox_cube(_vec3(bbox_min), _vec3(bbox_max), lo, hi), "cvx_bbox_cube")
+    return np.array(lo[:], dtype=np.float32), np.array(hi[:], dtype=np.float32)
+
+
+def mesh_bbox(triangles: np.ndarray):
+    t = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)
+    lo = (ctypes.c_float * 3)()
+    hi = (ctypes.c_float * 3)()
+    check(lib.cvx_mesh_bbox(t.ctypes.data, t.shape[0], lo, hi), "cvx_mesh_bbox")
+    return np.array(lo[:], dtype=np.float32), np.array(hi[:], dtype=np.float32)
+
+
+def make_voxinfo(triangles: np.ndarray, gridsize) -> VoxInfo:
+    """What the reference's main() does (src/main.cpp:179-186): vertex bbox, padded to a cube,
+    then the voxinfo for a gridsize^3 grid."""
+    t = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, 9)
+    lo, hi = mesh_bbox(t)
+    clo, chi = create_mesh_bbox_cube(lo, hi)
+    return make_info(clo, chi, gridsize, t.shape[0])
+
+
+def table_words(info: VoxInfo) -> int:
+    return int(lib.cvx_table_words(ctypes.byref(info)))
+
+
+def _ptr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("device buffers must be CUDA tensors (or raw device pointers)")
+        if not x.is_contiguous():
+            raise ValueError("device buffers must be contiguous")
+        return int(x.data_ptr())
+    raise TypeError(f"cannot take a device pointer of {type(x)}")
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        import torch
+        return int(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)
+
+
+def _check_sizes(info: VoxInfo, triangle_data, vtable) -> None:
+    if hasattr(triangle_data, "numel") and triangle_data.numel() < 9 * info.n_triangles:
+        raise ValueError(f"triangle_data holds {triangle_data.numel()} floats, need {9 * info.n_triangles}")
+    if hasattr(vtable, "numel") and vtable.numel() * vtable.element_size() < 4 * table_words(info):
+        raise ValueError(f"vtable holds {vtable.numel() * vtable.element_size()} bytes, "
+                         f"need {4 * table_words(info)}")
+
+
+def voxelize(info: VoxInfo, triangle_data, vtable, morton_code: bool = False, stream=None) -> None:
+    """Surface voxelization into ``vtable`` (ORs bits in; zero it first), asynchronous on ``stream``
+    (default: torch's current stream)."""
+    _check_sizes(info, triangle_data, vtable)
+    check(lib.cvx_voxelize(ctypes.byref(info), _ptr(triangle_data), _ptr(vtable), int(bool(morton_code)),
+                           _stream(stream)), "cvx_voxelize")
+
+
+def voxelize_solid(info: VoxInfo, triangle_data, vtable, morton_code: bool = False, stream=None) -> None:
+    """Solid voxelization into ``vtable`` (XORs bits in; zero it first)."""
+    _check_sizes(info, triangle_data, vtable)
+    check(lib.cvx_voxelize_solid(ctypes.byref(info), _ptr(triangle_data), _ptr(vtable), int(bool(morton_code)),
+                                 _stream(stream)), "cvx_voxelize_solid")
+
+
+def workspace_size(info: VoxInfo, solid: bool) -> int:
+    return int(lib.cvx_workspace_size(ctypes.byref(info), int(bool(solid))))
+
+
+def voxelize_ws(info: VoxInfo, triangle_data, vtable, workspace, morton_code=False, solid=False, stream=None):
+    """Voxelize with caller-owned scratch (a CUDA tensor of at least workspace_size() bytes)."""
+    _check_sizes(info, triangle_data, vtable)
+    nbytes = workspace.numel() * workspace.element_size() if hasattr(workspace, "numel") else 1 << 62
+    check(lib.cvx_voxelize_ws(ctypes.byref(info), _ptr(triangle_data), _ptr(vtable), int(bool(morton_code)),
+                              int(bool(solid)), _ptr(workspace), int(nbytes), _stream(stream)), "cvx_voxelize_ws")
+
+
+def device_status(stream=None) -> None:
+    check(lib.cvx_device_status(_stream(stream)), "cvx_device_status")
+
+
+@dataclass
+class Job:
+    """One mesh of a batch: its voxinfo, device triangles and table, and mode."""
+
+    info: VoxInfo
+    triangles: object
+    table: object
+    morton: bool = False
+    solid: bool = False
+
+
+def _jobs_array(jobs: Sequence[Job]):
+    arr = (CvxJob * max(1, len(jobs)))()
+    for i, j in enumerate(jobs):
+        _check_sizes(j.info, j.triangles, j.table)
+        arr[i].info = j.info
+        arr[i].d_triangles = _ptr(j.triangles)
+        arr[i].d_table = _ptr(j.table)
+        arr[i].morton = int(bool(j.morton))
+        arr[i].solid = int(bool(j.solid))
+    return arr
+
+
+def voxelize_batch(jobs: Sequence[Job], stream=None) -> None:
+    """All jobs in one launch sequence; bit-identical to one voxelize / voxelize_solid per job."""
+    arr = _jobs_array(jobs)
+    check(lib.cvx_voxelize_batch(arr, len(jobs), _stream(stream)), "cvx_voxelize_batch")
+
+
+class Plan:
+    """A batch captured once into a CUDA graph and replayed with one launch."""
+
+    CLEAR_TABLES = 1
+
+    def __init__(self, jobs: Sequence[Job], clear_tables: bool = True):
+        self._jobs = list(jobs)  # keep buffers alive
+        arr = _jobs_array(self._jobs)
+        h = ctypes.c_void_p()
+        check(lib.cvx_plan_create(arr, len(self._jobs), self.CLEAR_TABLES if clear_tables else 0, ctypes.byref(h)),
+              "cvx_plan_create")
+        self._h = h
+
+    def launch(self, stream=None) -> None:
+        check(lib.cvx_plan_launch(self._h, _stream(stream)), "cvx_plan_launch")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.cvx_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def get_tuning(device: int = 0) -> dict:
+    t = CvxTuning()
+    check(lib.cvx_get_tuning(device, ctypes.byref(t)), "cvx_get_tuning")
+    return {"small_vox": t.small_vox, "small_cols": t.small_cols}
+
+
+def set_tuning(device: int = 0, small_vox: int | None = None, small_cols: int | None = None) -> None:
+    cur = get_tuning(device)
+    t = CvxTuning(small_vox if small_vox is not None else cur["small_vox"],
+                  small_cols if small_cols is not None else cur["small_cols"])
+    check(lib.cvx_set_tuning(device, ctypes.byref(t)), "cvx_set_tuning")
+
+
+def voxelize_host(info: VoxInfo, triangles: np.ndarray, morton: bool = False, solid: bool = False) -> np.ndarray:
+    """Host arrays in, host table out: copies the soup to the device, voxelizes into a zeroed table
+    and copies it back (what the reference's main() does around voxelize, src/main.cpp:205-222)."""
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1)).cuda()
+    table = torch.zeros(table_words(info), dtype=torch.int32, device="cuda")
+    (voxelize_solid if solid else voxelize)(info, t, table, morton)
+    return table.cpu().numpy().view(np.uint32)

@@ -1,0 +1,774 @@
+// api.cu -- C ABI of the engine (include/cvx.h): validation, scratch management, launch grouping,
+// batches and graph-captured plans.
+//
+// Scratch.  Every launch sequence needs a small counter block, a queue of triangle records (at
+// most one per triangle) and, for solid voxelization, a linear-order flip table per job.  The
+// library keeps one scratch set per (device, stream), grown on demand; the flip tables are zeroed
+// when allocated and every solid launch leaves them zero again, so no per-call clearing is
+// needed.  cvx_voxelize_ws takes caller-owned scratch instead (and clears its flip region).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "cvx.h"
+#include "engine.h"
+
+using namespace cvx;
+
+static_assert(sizeof(cvx_voxinfo) == 64, "cvx_voxinfo must match the reference voxinfo (64 bytes)");
+static_assert(offsetof(cvx_voxinfo, gridsize) == 24, "voxinfo.gridsize offset");
+static_assert(offsetof(cvx_voxinfo, n_triangles) == 40, "voxinfo.n_triangles offset");
+static_assert(offsetof(cvx_voxinfo, unit) == 48, "voxinfo.unit offset");
+
+namespace {
+
+thread_local std::string g_msg;
+
+cvx_status fail(cvx_status s, const char* fmt, ...) {
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	std::vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	g_msg = buf;
+	return s;
+}
+
+cvx_status cuda_fail(cudaError_t e, const char* where) {
+	return fail(CVX_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+#define CVX_CUDA(call)                                   \
+	do {                                                 \
+		cudaError_t e_ = (call);                         \
+		if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+	} while (0)
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
+
+struct DevState {
+	int sms = 0;
+	int rows_grid = 0;
+	int cols_grid = 0;
+	Tune tune;
+};
+
+std::mutex g_mu;
+std::map<int, DevState> g_dev;
+
+cvx_status dev_state(DevState& out, int* dev_out = nullptr) {
+	int dev = 0;
+	CVX_CUDA(cudaGetDevice(&dev));
+	std::lock_guard<std::mutex> lk(g_mu);
+	auto it = g_dev.find(dev);
+	if (it == g_dev.end()) {
+		DevState d;
+		CVX_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
+		d.rows_grid = d.sms * surf_rows_blocks_per_sm();
+		d.cols_grid = d.sms * solid_cols_blocks_per_sm();
+		it = g_dev.emplace(dev, d).first;
+	}
+	out = it->second;
+	if (dev_out) *dev_out = dev;
+	return CVX_OK;
+}
+
+// ---- scratch ------------------------------------------------------------------------------------
+
+struct RecLayout {
+	size_t ctr, big, mid, jobs, end;
+};
+RecLayout rec_layout(uint64_t cap, uint64_t n_jobs) {
+	RecLayout l;
+	l.ctr = 0;
+	l.big = align_up(sizeof(Counters));
+	l.mid = align_up(l.big + cap * sizeof(BigRec));
+	l.jobs = align_up(l.mid + cap * sizeof(MidRec));
+	l.end = align_up(l.jobs + n_jobs * sizeof(JobDesc));
+	return l;
+}
+
+struct StreamScratch {
+	void* rec = nullptr;
+	size_t rec_bytes = 0;
+	uint32_t* flips = nullptr;  // zero between launch sequences
+	size_t flip_bytes = 0;
+	JobDesc* staging = nullptr; // pinned host copy of uploaded job arrays
+	size_t staging_n = 0;
+	cudaEvent_t staging_done = nullptr;
+};
+std::map<std::pair<int, cudaStream_t>, StreamScratch> g_ws;
+
+bool capturing(cudaStream_t s) {
+	cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+	if (cudaStreamIsCapturing(s, &st) != cudaSuccess) return false;
+	return st != cudaStreamCaptureStatusNone;
+}
+
+cvx_status ensure_scratch(int dev, cudaStream_t s, size_t rec_bytes, size_t flip_bytes, size_t staging_n,
+                          StreamScratch** out) {
+	std::lock_guard<std::mutex> lk(g_mu);
+	StreamScratch& w = g_ws[{dev, s}];
+	const bool grow_rec = rec_bytes > w.rec_bytes, grow_flip = flip_bytes > w.flip_bytes;
+	const bool grow_stage = staging_n > w.staging_n;
+	if ((grow_rec || grow_flip || grow_stage) && capturing(s))
+		return fail(CVX_ERR_CAPTURING, "scratch must grow while the stream is being captured; make one call before capture "
+		                               "or use cvx_voxelize_ws");
+	if (grow_rec || grow_flip) CVX_CUDA(cudaStreamSynchronize(s));
+	if (grow_rec) {
+		if (w.rec) cudaFree(w.rec);
+		w.rec = nullptr;
+		w.rec_bytes = 0;
+		size_t b = std::max(rec_bytes, (size_t)1 << 20);
+		if (cudaMalloc(&w.rec, b) != cudaSuccess) {
+			cudaGetLastError();
+			return fail(CVX_ERR_OUT_OF_MEMORY, "cannot allocate %zu bytes of scratch", b);
+		}
+		w.rec_bytes = b;
+	}
+	if (grow_flip) {
+		if (w.flips) cudaFree(w.flips);
+		w.flips = nullptr;
+		w.flip_bytes = 0;
+		if (cudaMalloc((void**)&w.flips, flip_bytes) != cudaSuccess) {
+			cudaGetLastError();
+			return fail(CVX_ERR_OUT_OF_MEMORY, "cannot allocate %zu bytes of flip table", flip_bytes);
+		}
+		CVX_CUDA(cudaMemsetAsync(w.flips, 0, flip_bytes, s));
+		w.flip_bytes = flip_bytes;
+	}
+	if (grow_stage) {
+		if (w.staging) {
+			if (w.staging_done) cudaEventSynchronize(w.staging_done);
+			cudaFreeHost(w.staging);
+		}
+		w.staging = nullptr;
+		w.staging_n = 0;
+		size_t n = std::max<size_t>(staging_n, 64);
+		CVX_CUDA(cudaMallocHost((void**)&w.staging, n * sizeof(JobDesc)));
+		w.staging_n = n;
+		if (!w.staging_done) CVX_CUDA(cudaEventCreateWithFlags(&w.staging_done, cudaEventDisableTiming));
+	}
+	*out = &w;
+	return CVX_OK;
+}
+
+// ---- validation and job descriptors -------------------------------------------------------------
+
+uint64_t words_of(const cvx_voxinfo& v) {
+	const uint64_t bits = (uint64_t)v.gridsize[0] * v.gridsize[1] * v.gridsize[2];
+	return (bits + 31) / 32;
+}
+
+cvx_status validate(const cvx_voxinfo* info, const void* tris, const void* table, int morton) {
+	if (!info) return fail(CVX_ERR_INVALID_VALUE, "info is null");
+	for (int i = 0; i < 3; i++) {
+		if (info->gridsize[i] == 0) return fail(CVX_ERR_INVALID_VALUE, "gridsize[%d] is 0", i);
+		if (info->gridsize[i] > (1u << 22)) return fail(CVX_ERR_UNSUPPORTED, "gridsize[%d] above 2^22", i);
+	}
+	if (info->n_triangles > 0 && !tris) return fail(CVX_ERR_INVALID_VALUE, "triangle pointer is null");
+	if (!table) return fail(CVX_ERR_INVALID_VALUE, "table pointer is null");
+	if (morton) {
+		const uint32_t g = info->gridsize[0];
+		// Morton codes of a g^3 grid fill [0, g^3) only for a cubic power-of-two grid; anything else
+		// addresses words beyond the table (the reference writes out of bounds there).
+		if (info->gridsize[1] != g || info->gridsize[2] != g || (g & (g - 1)) != 0)
+			return fail(CVX_ERR_UNSUPPORTED, "Morton order needs a cubic power-of-two grid (got %u x %u x %u)", g,
+			            info->gridsize[1], info->gridsize[2]);
+	}
+	return CVX_OK;
+}
+
+JobDesc make_job(const cvx_voxinfo& v, const float* tris, uint32_t* table, int morton, int solid) {
+	JobDesc j;
+	std::memset(&j, 0, sizeof(j));
+	j.tris = tris;
+	j.table = table;
+	j.n_tri = v.n_triangles;
+	for (int i = 0; i < 3; i++) {
+		j.bmin[i] = v.bbox_min[i];
+		j.unit[i] = v.unit[i];
+		j.grid[i] = v.gridsize[i];
+	}
+	j.flags = (morton ? JOB_MORTON : 0u) | (solid ? JOB_SOLID : 0u);
+	return j;
+}
+
+uint32_t tiles_of(uint64_t n) { return (uint32_t)((n + kTile - 1) / kTile); }
+
+// A group of jobs launched together (same mode), with prefix fields filled in.
+struct Group {
+	std::vector<JobDesc> jobs;
+	uint64_t tris = 0;
+	uint32_t tiles = 0, units = 0;
+	uint64_t mwords = 0;
+	uint64_t flip_words = 0;
+};
+
+void finish_group(Group& g, bool solid) {
+	uint32_t tile = 0, unit = 0;
+	uint64_t mw = 0;
+	g.tris = 0;
+	for (JobDesc& j : g.jobs) {
+		j.tile_begin = tile;
+		tile += tiles_of(j.n_tri);
+		g.tris += j.n_tri;
+		if (solid) {
+			j.unit_begin = unit;
+			unit += (uint32_t)solid_units(j.grid).units;
+			j.mword_begin = mw;
+			if (j.flags & JOB_MORTON) mw += ((uint64_t)j.grid[0] * j.grid[1] * j.grid[2] + 31) / 32;
+		}
+	}
+	g.tiles = tile;
+	g.units = unit;
+	g.mwords = mw;
+}
+
+// Split jobs of one mode into launch groups of fewer than kMaxTriPerLaunch triangles.  A job above
+// the limit is cut into triangle ranges (same table: the results accumulate exactly).
+std::vector<Group> make_groups(const std::vector<JobDesc>& jobs, bool solid) {
+	std::vector<Group> out;
+	Group cur;
+	for (const JobDesc& j0 : jobs) {
+		JobDesc j = j0;
+		uint64_t off = 0;
+		do {
+			JobDesc part = j;
+			const uint64_t room = kMaxTriPerLaunch - cur.tris;
+			const uint64_t take = std::min<uint64_t>(j.n_tri - off, room);
+			part.tris = j.tris + off * 9;
+			part.n_tri = take;
+			cur.jobs.push_back(part);
+			cur.tris += take;
+			off += take;
+			if (cur.tris >= kMaxTriPerLaunch) {
+				out.push_back(cur);
+				cur = Group();
+			}
+		} while (off < j.n_tri);
+	}
+	if (!cur.jobs.empty()) out.push_back(cur);
+	for (Group& g : out) finish_group(g, solid);
+	return out;
+}
+
+// Solid jobs whose resolve must follow all their toggle launches: one resolve group per distinct
+// table (jobs cut into ranges share one).
+Group resolve_group(const std::vector<JobDesc>& jobs) {
+	Group g;
+	g.jobs = jobs;
+	for (JobDesc& j : g.jobs) j.n_tri = 0;  // resolve only
+	finish_group(g, true);
+	return g;
+}
+
+uint64_t flip_bytes_of(const JobDesc& j) {
+	return align_up(((uint64_t)j.grid[0] * j.grid[1] * j.grid[2] + 31) / 32 * 4);
+}
+
+// Run every launch of a mixed job list on stream s using the scratch at (rec, flips).  `upload`
+// copies job arrays to the device (stream-ordered).
+struct Runner {
+	cudaStream_t s;
+	DevState dev;
+	char* rec;
+	size_t rec_bytes;
+	uint32_t* flips;  // solid flip tables, laid out back to back in job order
+	JobDesc* staging;
+	size_t staging_cap;
+	size_t staging_used = 0;
+	size_t jobs_used = 0;  // JobDesc slots used in the device job area
+	uint64_t cap;          // queue capacity (triangles)
+	size_t jobs_off;
+
+	cvx_status prepare(Group& g, LaunchDesc& L) {
+		std::memset(&L, 0, sizeof(L));
+		L.n_jobs = (uint32_t)g.jobs.size();
+		L.n_tiles = g.tiles;
+		L.n_units = g.units;
+		L.n_mwords = g.mwords;
+		L.scr.ctr = reinterpret_cast<Counters*>(rec);
+		const RecLayout lay = rec_layout(cap, 0);
+		L.scr.big = reinterpret_cast<BigRec*>(rec + lay.big);
+		L.scr.mid = reinterpret_cast<MidRec*>(rec + lay.mid);
+		L.scr.cap = (uint32_t)cap;
+		if (g.jobs.size() == 1) {
+			L.single = g.jobs[0];
+			L.jobs = nullptr;
+			return CVX_OK;
+		}
+		if (staging_used + g.jobs.size() > staging_cap) return fail(CVX_ERR_INVALID_VALUE, "job staging overflow");
+		JobDesc* host = staging + staging_used;
+		std::memcpy(host, g.jobs.data(), g.jobs.size() * sizeof(JobDesc));
+		JobDesc* devp = reinterpret_cast<JobDesc*>(rec + jobs_off) + jobs_used;
+		CVX_CUDA(cudaMemcpyAsync(devp, host, g.jobs.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, s));
+		staging_used += g.jobs.size();
+		jobs_used += g.jobs.size();
+		L.jobs = devp;
+		return CVX_OK;
+	}
+
+	cvx_status run(const std::vector<JobDesc>& surf, const std::vector<JobDesc>& solid) {
+		for (Group& g : make_groups(surf, false)) {
+			LaunchDesc L;
+			cvx_status st = prepare(g, L);
+			if (st != CVX_OK) return st;
+			CVX_CUDA(cudaMemsetAsync(rec, 0, kCountersResetBytes, s));
+			CVX_CUDA(launch_surface(L, dev.tune, dev.rows_grid, s));
+		}
+		if (!solid.empty()) {
+			for (Group& g : make_groups(solid, true)) {
+				LaunchDesc L;
+				cvx_status st = prepare(g, L);
+				if (st != CVX_OK) return st;
+				CVX_CUDA(cudaMemsetAsync(rec, 0, kCountersResetBytes, s));
+				CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidToggles));
+			}
+			Group r = resolve_group(solid);
+			LaunchDesc L;
+			cvx_status st = prepare(r, L);
+			if (st != CVX_OK) return st;
+			CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidResolve));
+		}
+		return CVX_OK;
+	}
+};
+
+// Number of JobDesc slots the uploads of run() need.
+size_t job_slots(const std::vector<JobDesc>& surf, const std::vector<JobDesc>& solid) {
+	size_t n = 0;
+	for (const Group& g : make_groups(surf, false)) n += g.jobs.size() > 1 ? g.jobs.size() : 0;
+	if (!solid.empty()) {
+		for (const Group& g : make_groups(solid, true)) n += g.jobs.size() > 1 ? g.jobs.size() : 0;
+		n += solid.size() > 1 ? solid.size() : 0;
+	}
+	return n;
+}
+
+uint64_t queue_cap(const std::vector<JobDesc>& a, const std::vector<JobDesc>& b) {
+	uint64_t m = 1;
+	for (const Group& g : make_groups(a, false)) m = std::max(m, g.tris);
+	for (const Group& g : make_groups(b, true)) m = std::max(m, g.tris);
+	return m;
+}
+
+// Assign each solid job its flip table inside one buffer.
+uint64_t assign_flips(std::vector<JobDesc>& solid, uint32_t* base) {
+	uint64_t off = 0;
+	for (JobDesc& j : solid) {
+		j.flips = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(base) + off);
+		off += flip_bytes_of(j);
+	}
+	return off;
+}
+
+cvx_status run_internal(std::vector<JobDesc> surf, std::vector<JobDesc> solid, cudaStream_t s) {
+	if (surf.empty() && solid.empty()) return CVX_OK;
+	DevState dev;
+	int devid = 0;
+	cvx_status st = dev_state(dev, &devid);
+	if (st != CVX_OK) return st;
+	uint64_t flip_total = 0;
+	for (const JobDesc& j : solid) flip_total += flip_bytes_of(j);
+	const uint64_t cap = queue_cap(surf, solid);
+	const size_t slots = job_slots(surf, solid);
+	const RecLayout lay = rec_layout(cap, slots);
+	StreamScratch* w = nullptr;
+	st = ensure_scratch(devid, s, lay.end, (size_t)flip_total, slots, &w);
+	if (st != CVX_OK) return st;
+	assign_flips(solid, w->flips);
+	if (slots && w->staging_done) CVX_CUDA(cudaEventSynchronize(w->staging_done));  // staging reusable
+	Runner r{s, dev, reinterpret_cast<char*>(w->rec), w->rec_bytes, w->flips, w->staging, w->staging_n};
+	r.cap = cap;
+	r.jobs_off = lay.jobs;
+	CVX_CUDA(cudaMemsetAsync(w->rec, 0, sizeof(Counters), s));
+	st = r.run(surf, solid);
+	if (st != CVX_OK) return st;
+	if (slots) CVX_CUDA(cudaEventRecord(w->staging_done, s));
+	return CVX_OK;
+}
+
+}  // namespace
+
+// ==== C ABI =======================================================================================
+
+extern "C" {
+
+const char* cvx_status_string(cvx_status s) {
+	switch (s) {
+	case CVX_OK: return "CVX_OK";
+	case CVX_ERR_INVALID_VALUE: return "CVX_ERR_INVALID_VALUE";
+	case CVX_ERR_UNSUPPORTED: return "CVX_ERR_UNSUPPORTED";
+	case CVX_ERR_OUT_OF_MEMORY: return "CVX_ERR_OUT_OF_MEMORY";
+	case CVX_ERR_CUDA: return "CVX_ERR_CUDA";
+	case CVX_ERR_DEVICE_CHECK: return "CVX_ERR_DEVICE_CHECK";
+	case CVX_ERR_CAPTURING: return "CVX_ERR_CAPTURING";
+	}
+	return "CVX_ERR_UNKNOWN";
+}
+
+const char* cvx_last_error_message(void) { return g_msg.c_str(); }
+
+int cvx_version(void) { return CVX_VERSION_MAJOR * 1000 + CVX_VERSION_MINOR; }
+
+cvx_status cvx_voxinfo_init(cvx_voxinfo* out, const float bbox_min[3], const float bbox_max[3],
+                            const uint32_t gridsize[3], uint64_t n_triangles) {
+	if (!out || !bbox_min || !bbox_max || !gridsize) return fail(CVX_ERR_INVALID_VALUE, "null argument");
+	std::memset(out, 0, sizeof(*out));
+	for (int i = 0; i < 3; i++) {
+		out->bbox_min[i] = bbox_min[i];
+		out->bbox_max[i] = bbox_max[i];
+		out->gridsize[i] = gridsize[i];
+		// src/util.h:58-60: (bbox.max - bbox.min) / float(gridsize)
+		volatile float ext = bbox_max[i] - bbox_min[i];
+		out->unit[i] = ext / (float)gridsize[i];
+	}
+	out->n_triangles = n_triangles;
+	return CVX_OK;
+}
+
+cvx_status cvx_bbox_cube(const float in_min[3], const float in_max[3], float out_min[3], float out_max[3]) {
+	if (!in_min || !in_max || !out_min || !out_max) return fail(CVX_ERR_INVALID_VALUE, "null argument");
+	// src/util.h:80-110, in float: lengths, max length via std::max, half-difference padding, then
+	// padding by extent / 10001 on every side.
+	volatile float len[3];
+	for (int i = 0; i < 3; i++) len[i] = in_max[i] - in_min[i];
+	const float myz = (len[1] < len[2]) ? len[2] : len[1];
+	const float mx = (len[0] < myz) ? myz : len[0];
+	float lo[3], hi[3];
+	for (int i = 0; i < 3; i++) {
+		lo[i] = in_min[i];
+		hi[i] = in_max[i];
+		if (mx != len[i]) {
+			volatile float delta = mx - len[i];
+			volatile float half = delta / 2.0f;
+			lo[i] = in_min[i] - half;
+			hi[i] = in_max[i] + half;
+		}
+	}
+	for (int i = 0; i < 3; i++) {
+		volatile float ext = hi[i] - lo[i];
+		volatile float eps = ext / 10001.0f;
+		out_min[i] = lo[i] - eps;
+		out_max[i] = hi[i] + eps;
+	}
+	return CVX_OK;
+}
+
+cvx_status cvx_mesh_bbox(const float* tris, uint64_t n, float out_min[3], float out_max[3]) {
+	if ((!tris && n) || !out_min || !out_max) return fail(CVX_ERR_INVALID_VALUE, "null argument");
+	if (n == 0) return fail(CVX_ERR_INVALID_VALUE, "empty mesh has no bounding box");
+	float lo[3] = {tris[0], tris[1], tris[2]}, hi[3] = {tris[0], tris[1], tris[2]};
+	for (uint64_t i = 0; i < 3 * n; i++) {
+		const float* v = tris + 3 * i;
+		for (int k = 0; k < 3; k++) {
+			lo[k] = v[k] < lo[k] ? v[k] : lo[k];
+			hi[k] = v[k] > hi[k] ? v[k] : hi[k];
+		}
+	}
+	for (int k = 0; k < 3; k++) {
+		out_min[k] = lo[k];
+		out_max[k] = hi[k];
+	}
+	return CVX_OK;
+}
+
+uint64_t cvx_table_words(const cvx_voxinfo* info) { return info ? words_of(*info) : 0; }
+
+cvx_status cvx_voxelize(const cvx_voxinfo* info, const float* d_tris, uint32_t* d_table, int morton,
+                        cvx_stream_t stream) {
+	cvx_status st = validate(info, d_tris, d_table, morton);
+	if (st != CVX_OK) return st;
+	if (info->n_triangles == 0) return CVX_OK;
+	std::vector<JobDesc> surf{make_job(*info, d_tris, d_table, morton, 0)}, solid;
+	return run_internal(surf, solid, (cudaStream_t)stream);
+}
+
+cvx_status cvx_voxelize_solid(const cvx_voxinfo* info, const float* d_tris, uint32_t* d_table, int morton,
+                              cvx_stream_t stream) {
+	cvx_status st = validate(info, d_tris, d_table, morton);
+	if (st != CVX_OK) return st;
+	if (info->n_triangles == 0) return CVX_OK;
+	std::vector<JobDesc> surf, solid{make_job(*info, d_tris, d_table, morton, 1)};
+	return run_internal(surf, solid, (cudaStream_t)stream);
+}
+
+uint64_t cvx_workspace_size(const cvx_voxinfo* info, int solid) {
+	if (!info) return 0;
+	const uint64_t n = std::max<uint64_t>(1, std::min<uint64_t>(info->n_triangles, kMaxTriPerLaunch));
+	const RecLayout lay = rec_layout(n, 0);
+	uint64_t b = lay.end;
+	if (solid) b += align_up(words_of(*info) * 4);
+	return b;
+}
+
+cvx_status cvx_voxelize_ws(const cvx_voxinfo* info, const float* d_tris, uint32_t* d_table, int morton, int solid,
+                           void* d_ws, uint64_t ws_bytes, cvx_stream_t stream) {
+	cvx_status st = validate(info, d_tris, d_table, morton);
+	if (st != CVX_OK) return st;
+	if (info->n_triangles == 0) return CVX_OK;
+	if (!d_ws) return fail(CVX_ERR_INVALID_VALUE, "workspace is null");
+	if (reinterpret_cast<uintptr_t>(d_ws) % kAlign) return fail(CVX_ERR_INVALID_VALUE, "workspace not 256-byte aligned");
+	const uint64_t need = cvx_workspace_size(info, solid);
+	if (ws_bytes < need) return fail(CVX_ERR_INVALID_VALUE, "workspace too small: %llu < %llu bytes",
+	                                 (unsigned long long)ws_bytes, (unsigned long long)need);
+	DevState dev;
+	st = dev_state(dev);
+	if (st != CVX_OK) return st;
+	cudaStream_t s = (cudaStream_t)stream;
+	const uint64_t cap = std::max<uint64_t>(1, std::min<uint64_t>(info->n_triangles, kMaxTriPerLaunch));
+	const RecLayout lay = rec_layout(cap, 0);
+	char* rec = static_cast<char*>(d_ws);
+	std::vector<JobDesc> surf, sol;
+	JobDesc j = make_job(*info, d_tris, d_table, morton, solid);
+	if (solid) {
+		j.flips = reinterpret_cast<uint32_t*>(rec + lay.end);
+		CVX_CUDA(cudaMemsetAsync(j.flips, 0, words_of(*info) * 4, s));
+		sol.push_back(j);
+	} else {
+		surf.push_back(j);
+	}
+	CVX_CUDA(cudaMemsetAsync(rec, 0, sizeof(Counters), s));
+	Runner r{s, dev, rec, (size_t)lay.end, j.flips, nullptr, 0};
+	r.cap = cap;
+	r.jobs_off = lay.jobs;
+	return r.run(surf, sol);
+}
+
+cvx_status cvx_device_status(cvx_stream_t stream) {
+	int dev = 0;
+	CVX_CUDA(cudaGetDevice(&dev));
+	cudaStream_t s = (cudaStream_t)stream;
+	CVX_CUDA(cudaStreamSynchronize(s));
+	void* rec = nullptr;
+	{
+		std::lock_guard<std::mutex> lk(g_mu);
+		auto it = g_ws.find({dev, s});
+		if (it == g_ws.end()) return CVX_OK;
+		rec = it->second.rec;
+	}
+	Counters c;
+	CVX_CUDA(cudaMemcpy(&c, rec, sizeof(c), cudaMemcpyDeviceToHost));
+	if (c.error) return fail(CVX_ERR_DEVICE_CHECK, "device check failed (code %u)", c.error);
+	return CVX_OK;
+}
+
+cvx_status cvx_voxelize_batch(const cvx_job* jobs, uint32_t n_jobs, cvx_stream_t stream) {
+	if (n_jobs && !jobs) return fail(CVX_ERR_INVALID_VALUE, "jobs is null");
+	std::vector<JobDesc> surf, solid;
+	for (uint32_t i = 0; i < n_jobs; i++) {
+		cvx_status st = validate(&jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton);
+		if (st != CVX_OK) return fail(st, "job %u: %s", i, g_msg.c_str());
+		JobDesc j = make_job(jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
+		if (jobs[i].info.n_triangles == 0) continue;
+		(jobs[i].solid ? solid : surf).push_back(j);
+	}
+	return run_internal(surf, solid, (cudaStream_t)stream);
+}
+
+// ---- plans: a batch captured once into a CUDA graph ----------------------------------------------
+
+struct cvx_plan {
+	cudaGraphExec_t exec = nullptr;
+	cudaGraph_t graph = nullptr;
+	void* rec = nullptr;
+	uint32_t* flips = nullptr;
+	JobDesc* staging = nullptr;
+};
+
+cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out) {
+	if (!out) return fail(CVX_ERR_INVALID_VALUE, "out is null");
+	*out = nullptr;
+	if (n_jobs && !jobs) return fail(CVX_ERR_INVALID_VALUE, "jobs is null");
+	std::vector<JobDesc> surf, solid;
+	std::vector<std::pair<uint32_t*, uint64_t>> tables;
+	for (uint32_t i = 0; i < n_jobs; i++) {
+		cvx_status st = validate(&jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton);
+		if (st != CVX_OK) return fail(st, "job %u: %s", i, g_msg.c_str());
+		tables.push_back({jobs[i].d_table, words_of(jobs[i].info)});
+		if (jobs[i].info.n_triangles == 0) continue;
+		JobDesc j = make_job(jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
+		(jobs[i].solid ? solid : surf).push_back(j);
+	}
+	DevState dev;
+	cvx_status st = dev_state(dev);
+	if (st != CVX_OK) return st;
+	cvx_plan* p = new cvx_plan();
+	auto bail = [&](cvx_status s2) {
+		cvx_plan_destroy(p);
+		return s2;
+	};
+	uint64_t flip_total = 0;
+	for (const JobDesc& j : solid) flip_total += flip_bytes_of(j);
+	const uint64_t cap = queue_cap(surf, solid);
+	const size_t slots = job_slots(surf, solid);
+	const RecLayout lay = rec_layout(cap, slots);
+	if (cudaMalloc(&p->rec, lay.end) != cudaSuccess) {
+		cudaGetLastError();
+		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
+	}
+	if (flip_total) {
+		if (cudaMalloc((void**)&p->flips, flip_total) != cudaSuccess) {
+			cudaGetLastError();
+			return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan flip tables"));
+		}
+		if (cudaMemset(p->flips, 0, flip_total) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "memset"));
+		assign_flips(solid, p->flips);
+	}
+	if (slots && cudaMallocHost((void**)&p->staging, slots * sizeof(JobDesc)) != cudaSuccess)
+		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan staging"));
+	cudaStream_t cs;
+	if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "stream"));
+	// Upload the job arrays once, outside the graph (the graph only reads them), in the order the
+	// capture below consumes them.
+	{
+		size_t used = 0;
+		auto upload = [&](const std::vector<Group>& gs) -> cvx_status {
+			for (const Group& g : gs) {
+				if (g.jobs.size() <= 1) continue;
+				JobDesc* devp = reinterpret_cast<JobDesc*>(static_cast<char*>(p->rec) + lay.jobs) + used;
+				if (cudaMemcpy(devp, g.jobs.data(), g.jobs.size() * sizeof(JobDesc), cudaMemcpyHostToDevice) != cudaSuccess)
+					return cuda_fail(cudaGetLastError(), "job upload");
+				used += g.jobs.size();
+			}
+			return CVX_OK;
+		};
+		cvx_status s2 = upload(make_groups(surf, false));
+		if (s2 == CVX_OK && !solid.empty()) s2 = upload(make_groups(solid, true));
+		if (s2 == CVX_OK && solid.size() > 1) {
+			std::vector<Group> rg{resolve_group(solid)};
+			s2 = upload(rg);
+		}
+		if (s2 != CVX_OK) {
+			cudaStreamDestroy(cs);
+			return bail(s2);
+		}
+	}
+	if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+		cudaStreamDestroy(cs);
+		return bail(cuda_fail(cudaGetLastError(), "begin capture"));
+	}
+	cvx_status cst = CVX_OK;
+	if (flags & CVX_PLAN_CLEAR_TABLES)
+		for (auto& t : tables)
+			if (cst == CVX_OK && cudaMemsetAsync(t.first, 0, t.second * 4, cs) != cudaSuccess)
+				cst = cuda_fail(cudaGetLastError(), "table clear");
+	if (cst == CVX_OK && cudaMemsetAsync(p->rec, 0, sizeof(Counters), cs) != cudaSuccess)
+		cst = cuda_fail(cudaGetLastError(), "counter clear");
+	if (cst == CVX_OK) {
+		// Launch exactly like Runner::run, but with the job arrays already resident.
+		size_t used = 0;
+		auto prep = [&](Group& g, LaunchDesc& L) {
+			std::memset(&L, 0, sizeof(L));
+			L.n_jobs = (uint32_t)g.jobs.size();
+			L.n_tiles = g.tiles;
+			L.n_units = g.units;
+			L.n_mwords = g.mwords;
+			L.scr.ctr = reinterpret_cast<Counters*>(p->rec);
+			const RecLayout l0 = rec_layout(cap, 0);
+			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(p->rec) + l0.big);
+			L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(p->rec) + l0.mid);
+			L.scr.cap = (uint32_t)cap;
+			if (g.jobs.size() == 1) {
+				L.single = g.jobs[0];
+			} else {
+				L.jobs = reinterpret_cast<JobDesc*>(static_cast<char*>(p->rec) + lay.jobs) + used;
+				used += g.jobs.size();
+			}
+		};
+		for (Group& g : make_groups(surf, false)) {
+			LaunchDesc L;
+			prep(g, L);
+			if (cudaMemsetAsync(p->rec, 0, kCountersResetBytes, cs) != cudaSuccess ||
+			    launch_surface(L, dev.tune, dev.rows_grid, cs) != cudaSuccess) {
+				cst = cuda_fail(cudaGetLastError(), "capture surface");
+				break;
+			}
+		}
+		if (cst == CVX_OK && !solid.empty()) {
+			for (Group& g : make_groups(solid, true)) {
+				LaunchDesc L;
+				prep(g, L);
+				if (cudaMemsetAsync(p->rec, 0, kCountersResetBytes, cs) != cudaSuccess ||
+				    launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidToggles) != cudaSuccess) {
+					cst = cuda_fail(cudaGetLastError(), "capture solid");
+					break;
+				}
+			}
+			if (cst == CVX_OK) {
+				Group rg = resolve_group(solid);
+				LaunchDesc L;
+				prep(rg, L);
+				if (launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidResolve) != cudaSuccess)
+					cst = cuda_fail(cudaGetLastError(), "capture resolve");
+			}
+		}
+	}
+	cudaGraph_t graph = nullptr;
+	cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+	cudaStreamDestroy(cs);
+	if (cst != CVX_OK) {
+		if (graph) cudaGraphDestroy(graph);
+		return bail(cst);
+	}
+	if (ee != cudaSuccess) return bail(cuda_fail(ee, "end capture"));
+	p->graph = graph;
+	if (cudaGraphInstantiate(&p->exec, graph, 0) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "instantiate"));
+	*out = p;
+	return CVX_OK;
+}
+
+cvx_status cvx_plan_launch(cvx_plan* p, cvx_stream_t stream) {
+	if (!p || !p->exec) return fail(CVX_ERR_INVALID_VALUE, "plan is null");
+	CVX_CUDA(cudaGraphLaunch(p->exec, (cudaStream_t)stream));
+	return CVX_OK;
+}
+
+cvx_status cvx_plan_destroy(cvx_plan* p) {
+	if (!p) return CVX_OK;
+	if (p->exec) cudaGraphExecDestroy(p->exec);
+	if (p->graph) cudaGraphDestroy(p->graph);
+	if (p->rec) cudaFree(p->rec);
+	if (p->flips) cudaFree(p->flips);
+	if (p->staging) cudaFreeHost(p->staging);
+	delete p;
+	return CVX_OK;
+}
+
+cvx_status cvx_get_tuning(int device, cvx_tuning* out) {
+	if (!out) return fail(CVX_ERR_INVALID_VALUE, "out is null");
+	std::lock_guard<std::mutex> lk(g_mu);
+	Tune t;
+	auto it = g_dev.find(device);
+	if (it != g_dev.end()) t = it->second.tune;
+	out->small_vox = t.small_vox;
+	out->small_cols = t.small_cols;
+	return CVX_OK;
+}
+
+cvx_status cvx_set_tuning(int device, const cvx_tuning* in) {
+	if (!in) return fail(CVX_ERR_INVALID_VALUE, "in is null");
+	int cur = 0;
+	CVX_CUDA(cudaGetDevice(&cur));
+	if (cur != device) CVX_CUDA(cudaSetDevice(device));
+	DevState d;
+	cvx_status st = dev_state(d);
+	if (cur != device) cudaSetDevice(cur);
+	if (st != CVX_OK) return st;
+	std::lock_guard<std::mutex> lk(g_mu);
+	g_dev[device].tune.small_vox = in->small_vox;
+	g_dev[device].tune.small_cols = in->small_cols;
+	return CVX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+// cvx_device.cuh -- device-side building blocks shared by the surface and solid engines.
+//
+// Exactness contract.  Every predicate of the reference kernels (src/voxelize.cu:58-190,
+// src/voxelize_solid.cu:16-145) is re-evaluated here with the same operands, the same operation
+// order and the same rounding: each multiply, add and fused multiply-add is written as an explicit
+// __fmul_rn / __fadd_rn / __fmaf_rn, so the compiler cannot contract or reorder them, and the
+// fused-multiply-add pattern is the one nvcc produces for the reference's helper_math expressions
+// on sm_103a (class RefFma below).  rsqrtf, IEEE division (__fdiv_rn), fminf/fmaxf and the
+// float->int conversions are the same device operations the reference compiles to.  Any
+// re-organisation the engine does (row intervals, column queues, parity flips) only changes
+// *which* voxels are evaluated and in what order, never the value of a predicate at a voxel.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cvx {
+
+// ------------------------------------------------------------------------------------------------
+// Fused-multiply-add pattern of the reference kernels (as compiled by nvcc --fmad=true).
+// Values follow the oracle's ovx_mode (oracle/cvx_oracle.c): 1 = the first product of a*b+c*d is
+// fused, fma(a,b,c*d); 2 = the second, fma(c,d,a*b).
+struct RefFma {
+	static constexpr int cross = 1;    // helper_math cross(): a.y*b.z - a.z*b.y -> fma(a.y,b.z,-(a.z*b.y))
+	static constexpr int dot3 = 1;     // helper_math dot(float3): fma(z,z',fma(x,x',y*y'))
+	static constexpr int dot2 = 1;     // helper_math dot(float2) in the triangle setup: fma(x,x',y*y')
+	static constexpr int plane = 1;    // per-voxel dot(n,p): 1 fma(nz,pz,fma(nx,px,ny*py)); 2 fma(nx,px,ny*py)+nz*pz
+	static constexpr int edge_xy = 1;  // per-voxel dot(n_xy_e, p_xy)
+	static constexpr int edge_yz = 1;  // per-voxel dot(n_yz_e, p_yz)
+	static constexpr int edge_zx = 1;  // per-voxel dot(n_zx_e, p_zx)
+	static constexpr int ccw = 1;      // solid checkCCW / check_point_triangle a*b-c*d
+	static constexpr int getx = 1;     // solid get_x_coordinate n.y*A + n.z*B
+};
+
+template <int P>
+__device__ __forceinline__ float mul_sub(float a, float b, float c, float d) {
+	if constexpr (P == 1) return __fmaf_rn(a, b, -__fmul_rn(c, d));
+	else if constexpr (P == 2) return __fmaf_rn(-c, d, __fmul_rn(a, b));
+	else return __fsub_rn(__fmul_rn(a, b), __fmul_rn(c, d));
+}
+template <int P>
+__device__ __forceinline__ float mul_add(float a, float b, float c, float d) {
+	if constexpr (P == 1) return __fmaf_rn(a, b, __fmul_rn(c, d));
+	else if constexpr (P == 2) return __fmaf_rn(c, d, __fmul_rn(a, b));
+	else return __fadd_rn(__fmul_rn(a, b), __fmul_rn(c, d));
+}
+template <int P>
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+	if constexpr (P == 1) return __fmaf_rn(az, bz, __fmaf_rn(ax, bx, __fmul_rn(ay, by)));
+	else if constexpr (P == 2) return __fmaf_rn(az, bz, __fmaf_rn(ay, by, __fmul_rn(ax, bx)));
+	else return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Job and launch descriptors.
+
+enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u };
+
+// One mesh voxelization.  Plain data, uploaded as an array for batches or passed by value for a
+// single mesh.
+struct JobDesc {
+	const float* tris;     // 9 floats per triangle (v0.xyz, v1.xyz, v2.xyz), device memory
+	uint32_t* table;       // destination bit table, ceil(gx*gy*gz/32) words, OR (surface) / XOR (solid)
+	uint32_t* flips;       // solid only: linear-order toggle table, zero on entry and left zero
+	uint64_t n_tri;
+	float bmin[3];
+	float unit[3];
+	uint32_t grid[3];
+	uint32_t flags;        // JOB_MORTON | JOB_SOLID
+	uint32_t tile_begin;   // first triangle tile of this job in the launch's tile space
+	uint32_t unit_begin;   // solid: first resolve unit of this job in the launch's unit space
+	uint64_t mword_begin;  // solid Morton: first Morton word of this job in the launch's word space
+};
+
+// Work-queue records written by the classify kernels and consumed by the cooperative kernels.
+struct BigRec {            // triangle whose work is split into several items
+	uint64_t item_begin;
+	uint32_t job, tri, n_items, pad;
+};
+struct MidRec {            // triangle handled as a single item
+	uint32_t job, tri;
+};
+
+// Device counters; zeroed before every launch sequence.
+// `big` packs (number of BigRec << 40) | (number of big items) so that one 64-bit atomic hands a
+// warp both its record slots and its item range; records are then sorted by item_begin, which
+// the consumer's binary search relies on.  A launch holds fewer than 2^24 triangles (the host
+// splits larger ones), so neither field can overflow into the other.
+constexpr int kBigShift = 40;
+constexpr unsigned long long kBigItemMask = (1ull << kBigShift) - 1ull;
+struct Counters {
+	unsigned long long big;
+	unsigned long long ticket;   // next work ticket of the cooperative kernel
+	unsigned int mid;            // number of MidRec
+	unsigned int error;          // nonzero: a device-side check failed (value says which)
+	unsigned int pad[2];
+};
+constexpr size_t kCountersResetBytes = 20;  // big, ticket, mid: reset before every launch sequence
+
+struct Scratch {
+	Counters* ctr;
+	BigRec* big;
+	MidRec* mid;
+	uint32_t cap;          // capacity of big[] and mid[] (>= triangles in the launch)
+};
+
+struct LaunchDesc {
+	const JobDesc* jobs;   // device array of n_jobs descriptors (n_jobs > 1)
+	JobDesc single;        // the descriptor itself when n_jobs == 1
+	uint32_t n_jobs;
+	uint32_t n_tiles;      // total triangle tiles over all jobs
+	uint32_t n_units;      // solid resolve units over all jobs
+	uint32_t pad;
+	uint64_t n_mwords;     // solid Morton words over all jobs
+	Scratch scr;
+};
+
+__device__ __forceinline__ const JobDesc& job_at(const LaunchDesc& L, uint32_t j) {
+	return L.n_jobs == 1 ? L.single : L.jobs[j];
+}
+
+// Job owning triangle tile `tile` (jobs are sorted by tile_begin).
+__device__ __forceinline__ uint32_t job_of_tile(const LaunchDesc& L, uint32_t tile) {
+	if (L.n_jobs == 1) return 0;
+	uint32_t lo = 0, hi = L.n_jobs - 1;
+	while (lo < hi) {
+		uint32_t mid = (lo + hi + 1) >> 1;
+		if (L.jobs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Morton order.  The reference encodes through three 256-entry LUTs (src/voxelize.cuh:20-34) whose
+// values are the 3-way bit spread of the byte (x -> bits 0,3,6,..; y -> 1,4,..; z -> 2,5,..).  For
+// coordinates below 2^16 (every grid whose table fits in memory) that equals the bit spread below.
+
+__device__ __forceinline__ uint64_t spread3(uint32_t v) {
+	uint64_t x = v & 0xFFFFu;
+	x = (x | (x << 16)) & 0x0000FF0000FFull;
+	x = (x | (x << 8)) & 0x00F00F00F00Full;
+	x = (x | (x << 4)) & 0x0C30C30C30C3ull;
+	x = (x | (x << 2)) & 0x249249249249ull;
+	return x;
+}
+__device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+	return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+__device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+// Bit layout (src/voxelize.cu:50-55): word = idx / 32, bit = 31 - idx % 32 (MSB first).
+__device__ __forceinline__ uint32_t bit_of(uint64_t idx) { return 0x80000000u >> (uint32_t)(idx & 31u); }
+
+// Mask of bit positions [a, b] (0 <= a <= b <= 31, counted MSB first) within one word.
+__device__ __forceinline__ uint32_t span_mask(uint32_t a, uint32_t b) {
+	return (0xFFFFFFFFu >> a) & (0xFFFFFFFFu << (31u - b));
+}
+
+// OR bits [lo, hi] of the linear bit stream into the table, one atomic per word.
+__device__ __forceinline__ void or_span(uint32_t* table, uint64_t lo, uint64_t hi) {
+	uint64_t w0 = lo >> 5, w1 = hi >> 5;
+	for (uint64_t w = w0; w <= w1; w++) {
+		uint32_t a = (w == w0) ? (uint32_t)(lo & 31u) : 0u;
+		uint32_t b = (w == w1) ? (uint32_t)(hi & 31u) : 31u;
+		atomicOr(table + w, span_mask(a, b));
+	}
+}
+
+// OR the Morton-ordered bits of row (y, z), x in [xl, xh], one atomic per touched word.  Within a
+// Morton word (32 consecutive codes) x varies in its two low bits only: codes of x = 4k..4k+3 sit at
+// offsets {0, 1, 8, 9} from the code of x = 4k.
+__device__ __forceinline__ void or_span_morton(uint32_t* table, int xl, int xh, uint32_t y, uint32_t z) {
+	const uint64_t yz = (spread3(y) << 1) | (spread3(z) << 2);
+	for (int k = xl >> 2; k <= (xh >> 2); k++) {
+		uint64_t code = spread3((uint32_t)(k << 2)) | yz;
+		uint32_t base = (uint32_t)(code & 31u);
+		uint32_t m = 0;
+		int j0 = max(xl - (k << 2), 0), j1 = min(xh - (k << 2), 3);
+		for (int j = j0; j <= j1; j++) m |= 0x80000000u >> (base + (uint32_t)(j & 1) + 8u * (uint32_t)(j >> 1));
+		atomicOr(table + (code >> 5), m);
+	}
+}
+
+// Last job whose range [begin, ...) starts at or before idx, for any monotone per-job begin field.
+template <class F>
+__device__ __forceinline__ uint32_t job_search(const LaunchDesc& L, uint64_t idx, F begin_of) {
+	if (L.n_jobs == 1) return 0;
+	uint32_t lo = 0, hi = L.n_jobs - 1;
+	while (lo < hi) {
+		uint32_t mid = (lo + hi + 1) >> 1;
+		if (begin_of(L.jobs[mid]) <= idx) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+__device__ __forceinline__ void set_error(const LaunchDesc& L, unsigned code) {
+	atomicCAS(&L.scr.ctr->error, 0u, code);
+}
+
+}  // namespace cvx

@@ -1,0 +1,46 @@
+// engine.h -- internal interface between the C-ABI layer (api.cu) and the kernel files.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "cvx_device.cuh"
+
+namespace cvx {
+
+constexpr uint32_t kTile = 256;        // triangles per classify CTA (one tile)
+constexpr uint32_t kZch = 32;          // z-slices per surface work item (one per lane)
+constexpr uint32_t kRowsThreads = 256; // threads per cooperative CTA
+constexpr uint32_t kColsPerItem = 256; // solid columns per work item
+
+// Device-side check codes written to Counters::error.
+enum : unsigned { kErrBulkTimeout = 1u, kErrQueueOverflow = 2u };
+
+// Triangles per launch sequence (the queue counters assume fewer than 2^24); larger meshes and
+// batches are split by the host.
+constexpr uint64_t kMaxTriPerLaunch = (1ull << 24) - 1;
+
+// Tunables (picked per device by the autotuner; defaults are safe everywhere).
+struct Tune {
+	uint32_t small_vox = 64;    // surface: bbox voxels at or below which a triangle stays in its thread
+	uint32_t small_cols = 32;   // solid: columns at or below which a triangle stays in its thread
+};
+
+// Surface launch sequence: classify + cooperative rows.  Counters must be zero.
+cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s);
+int surf_rows_blocks_per_sm();
+
+// Solid launch sequence.  kSolidToggles: classify + cooperative columns (counters must be zero);
+// kSolidResolve: prefix-XOR resolve into the tables (+ Morton transcode).  Every job's flips table
+// must be zero before the toggles and is zero again after the resolve.
+enum : unsigned { kSolidToggles = 1u, kSolidResolve = 2u };
+cudaError_t launch_solid(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases);
+int solid_cols_blocks_per_sm();
+
+// Resolve-unit bookkeeping of a solid job: rows per unit and units per job.
+struct SolidUnits {
+	uint64_t rows_per_unit;
+	uint64_t units;
+	bool aligned;   // gx % 32 == 0: rows start on word boundaries
+};
+SolidUnits solid_units(const uint32_t grid[3]);
+
+}  // namespace cvx

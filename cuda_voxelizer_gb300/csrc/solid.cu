@@ -1,0 +1,538 @@
+// solid.cu -- solid voxelization kernels (reference: voxelize_triangle_solid,
+// src/voxelize_solid.cu:16-145).
+//
+// The reference casts, for every voxel-centre column (y, z) inside a triangle's YZ projection, the
+// column onto the triangle's plane and XORs every voxel x in [0, xmax] (:115-135): O(g) single-bit
+// atomics per column hit, and parity along +x yields the solid.  The engine computes the same
+// column hits with the same arithmetic, but records each hit as two toggles in a linear-order flip
+// table (the start of the row and xmax + 1), then resolves all rows with one prefix-XOR pass and
+// XORs the resolved bits into the caller's table (or scatters them into Morton order).  The XOR of
+// any set of [0, xmax] ranges is exactly what this produces.
+//
+// Kernels, in launch order:
+//   solid_classify  one CTA per 256-triangle tile (TMA bulk staging as in surface.cu); triangles
+//                   with at most `small_cols` columns are finished in the thread, others queued.
+//   solid_cols      persistent; each warp takes an item of up to kColsPerItem columns.
+//   solid_resolve   one warp per resolve unit (whole rows): segmented prefix XOR along x.
+//   solid_morton    Morton jobs only: gathers resolved linear bits into Morton words.
+//   solid_zero      Morton jobs only: clears the flip table (the transcode reads it shared).
+#include "engine.h"
+
+namespace cvx {
+
+namespace {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+constexpr double kFloatError = 0.000001;  // src/voxelize_solid.cu:13 (a double literal)
+
+struct SolidTri {
+	float nx, ny, nz;
+	float v0x, v0y, v0z;
+	float ax, ay, bx, by, cx, cy;  // v0_yz, v1_yz, v2_yz after the counter-clockwise swap
+	int y0, y1, z0, z1;            // column range, clipped to the grid
+	bool skip;
+};
+
+// Triangle setup, src/voxelize_solid.cu:83-119.
+template <class P>
+__device__ __forceinline__ void solid_setup(const float* t, const float* bmin, const float* unit, const uint32_t* grid,
+                                            SolidTri& S) {
+	const float v0x = __fsub_rn(t[0], bmin[0]), v0y = __fsub_rn(t[1], bmin[1]), v0z = __fsub_rn(t[2], bmin[2]);
+	const float v1x = __fsub_rn(t[3], bmin[0]), v1y = __fsub_rn(t[4], bmin[1]), v1z = __fsub_rn(t[5], bmin[2]);
+	const float v2x = __fsub_rn(t[6], bmin[0]), v2y = __fsub_rn(t[7], bmin[1]), v2z = __fsub_rn(t[8], bmin[2]);
+	const float e0x = __fsub_rn(v1x, v0x), e0y = __fsub_rn(v1y, v0y), e0z = __fsub_rn(v1z, v0z);
+	const float e1x = __fsub_rn(v2x, v1x), e1y = __fsub_rn(v2y, v1y), e1z = __fsub_rn(v2z, v1z);
+	const float cx = mul_sub<P::cross>(e0y, e1z, e0z, e1y);
+	const float cy = mul_sub<P::cross>(e0z, e1x, e0x, e1z);
+	const float cz = mul_sub<P::cross>(e0x, e1y, e0y, e1x);
+	const float inv = rsqrtf(dot3<P::dot3>(cx, cy, cz, cx, cy, cz));
+	S.nx = __fmul_rn(cx, inv);
+	S.ny = __fmul_rn(cy, inv);
+	S.nz = __fmul_rn(cz, inv);
+	S.v0x = v0x; S.v0y = v0y; S.v0z = v0z;
+	S.skip = (double)fabsf(S.nx) < kFloatError;  // :92 (the thread returns)
+	// YZ projection, made counter-clockwise (:95-105; checkCCW :55-64)
+	float ax = v0y, ay = v0z, bx = v1y, by = v1z, qx = v2y, qy = v2z;
+	const float ccw = mul_sub<P::ccw>(__fsub_rn(bx, ax), __fsub_rn(qy, ay), __fsub_rn(qx, ax), __fsub_rn(by, ay));
+	if (!(ccw > 0.0f)) {
+		float tx = bx, ty = by;
+		bx = qx; by = qy; qx = tx; qy = ty;
+	}
+	S.ax = ax; S.ay = ay; S.bx = bx; S.by = by; S.cx = qx; S.cy = qy;
+	// column range (:109-119): floor/ceil(q - 0.5) evaluated in double, loop y from (int)min while
+	// (float)y <= max.  Columns outside the grid are dropped (the reference writes them outside the
+	// table or into neighbouring rows).
+	const float mxy = fmaxf(ax, fmaxf(bx, qx)), mxz = fmaxf(ay, fmaxf(by, qy));
+	const float mny = fminf(ax, fminf(bx, qx)), mnz = fminf(ay, fminf(by, qy));
+	const float gmaxy = (float)floor((double)__fdiv_rn(mxy, unit[1]) - 0.5);
+	const float gmaxz = (float)floor((double)__fdiv_rn(mxz, unit[2]) - 0.5);
+	const float gminy = (float)ceil((double)__fdiv_rn(mny, unit[1]) - 0.5);
+	const float gminz = (float)ceil((double)__fdiv_rn(mnz, unit[2]) - 0.5);
+	int y0 = __float2int_rz(gminy), z0 = __float2int_rz(gminz);
+	// last integer y with (float)y <= gmax (gmax holds an integer value, or is not finite)
+	int y1 = gmaxy >= 2147483520.0f ? 2147483647 : (gmaxy >= -2147483648.0f ? (int)gmaxy : (-2147483647 - 1));
+	int z1 = gmaxz >= 2147483520.0f ? 2147483647 : (gmaxz >= -2147483648.0f ? (int)gmaxz : (-2147483647 - 1));
+	if (!(gmaxy == gmaxy)) y1 = y0 - 1;  // NaN bound: the loop never runs
+	if (!(gmaxz == gmaxz)) z1 = z0 - 1;
+	S.y0 = max(y0, 0); S.z0 = max(z0, 0);
+	S.y1 = min(y1, (int)grid[1] - 1); S.z1 = min(z1, (int)grid[2] - 1);
+}
+
+__device__ __forceinline__ bool top_left(float v0x, float v0y, float v1x, float v1y) {
+	return (v1y < v0y) || (v1y == v0y && v0x > v1x);  // :67-70
+}
+
+// Column test for voxel-centre column (y, z): returns true and xmax on a hit (:119-123).
+template <class P>
+__device__ __forceinline__ bool column_hit(const SolidTri& S, const float* unit, int y, int z, int& xmax) {
+	// ((y + 0.5) * unit.y) in double then rounded to float == the float product of the exact y+0.5f
+	// for |y| < 2^22 (the double product is exact, so both round the same real number once).
+	const float px = __fmul_rn(__int2float_rn(y) + 0.5f, unit[1]);
+	const float py = __fmul_rn(__int2float_rn(z) + 0.5f, unit[2]);
+	// check_point_triangle (:24-46)
+	const float PAx = __fsub_rn(px, S.ax), PAy = __fsub_rn(py, S.ay);
+	const float PBx = __fsub_rn(px, S.bx), PBy = __fsub_rn(py, S.by);
+	const float PCx = __fsub_rn(px, S.cx), PCy = __fsub_rn(py, S.cy);
+	int check;
+	const float t1 = mul_sub<P::ccw>(PAx, PBy, PAy, PBx);
+	const float t2 = mul_sub<P::ccw>(PBx, PCy, PBy, PCx);
+	const float t3 = mul_sub<P::ccw>(PCx, PAy, PCy, PAx);
+	if ((double)fabsf(t1) < kFloatError && __fmul_rn(PAx, PBx) <= 0.0f && __fmul_rn(PAy, PBy) <= 0.0f) check = 1;
+	else if ((double)fabsf(t2) < kFloatError && __fmul_rn(PBx, PCx) <= 0.0f && __fmul_rn(PBy, PCy) <= 0.0f) check = 2;
+	else if ((double)fabsf(t3) < kFloatError && __fmul_rn(PCx, PAx) <= 0.0f && __fmul_rn(PCy, PAy) <= 0.0f) check = 3;
+	else if (__fmul_rn(t1, t2) > 0.0f && __fmul_rn(t1, t3) > 0.0f) check = 0;
+	else check = -1;
+	const bool in = (check == 1 && top_left(S.ax, S.ay, S.bx, S.by)) || (check == 2 && top_left(S.bx, S.by, S.cx, S.cy)) ||
+	                (check == 3 && top_left(S.cx, S.cy, S.ax, S.ay)) || (check == 0);
+	if (!in) return false;
+	// get_x_coordinate (:49-52): -(n.y*(p.x - v0.y) + n.z*(p.y - v0.z)) / n.x + v0.x
+	const float m = mul_add<P::getx>(S.ny, __fsub_rn(px, S.v0y), S.nz, __fsub_rn(py, S.v0z));
+	const float xh = __fadd_rn(__fdiv_rn(-m, S.nx), S.v0x);
+	xmax = __double2int_rz((double)__fdiv_rn(xh, unit[0]) - 0.5);  // int(... / unit.x - 0.5)
+	return true;
+}
+
+__device__ __forceinline__ void toggle(uint32_t* flips, uint64_t bit) { atomicXor(flips + (bit >> 5), bit_of(bit)); }
+
+// Record column hit (y, z, xmax): the reference flips bits [0, xmax] of the column's row, i.e. the
+// linear bit range [r*gx, r*gx + xmax]; a range longer than the row continues into the following
+// rows (:124-135).  Morton order has no such continuation (x is encoded on its own), the range is
+// clipped at the row end there (beyond it the reference writes outside the table).
+__device__ __forceinline__ void record_hit(uint32_t* flips, const uint32_t* grid, bool morton, int y, int z, int xmax) {
+	if (xmax < 0) return;
+	const uint64_t gx = grid[0];
+	const uint64_t rows = (uint64_t)grid[1] * grid[2];
+	const uint64_t row = (uint64_t)y + (uint64_t)z * grid[1];
+	const uint64_t len = (uint64_t)xmax + 1;
+	if (morton || len <= gx) {
+		toggle(flips, row * gx);
+		const uint64_t e = len < gx ? len : gx;
+		if (e < gx) toggle(flips, row * gx + e);
+		return;
+	}
+	const uint64_t q = len / gx, rem = len % gx;
+	for (uint64_t k = 0; k < q && row + k < rows; k++) toggle(flips, (row + k) * gx);
+	if (rem && row + q < rows) {
+		toggle(flips, (row + q) * gx);
+		toggle(flips, (row + q) * gx + rem);
+	}
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+	for (uint32_t it = 0; it < (1u << 24); it++) {
+		uint32_t ok;
+		asm volatile(
+		    "{\n\t.reg .pred p;\n\t"
+		    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		    "selp.u32 %0, 1, 0, p;\n\t}"
+		    : "=r"(ok)
+		    : "r"(bar), "r"(parity)
+		    : "memory");
+		if (ok) return true;
+	}
+	return false;
+}
+
+__device__ __forceinline__ void stage_tile(const LaunchDesc& L, const float* src, uint32_t cnt, float* s_tri,
+                                           uint64_t* s_bar) {
+	const uint32_t bytes = cnt * 36u;
+	const bool bulk = cnt == kTile && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0);
+	if (bulk) {
+		const uint32_t bar = (uint32_t)__cvta_generic_to_shared(s_bar);
+		const uint32_t dst = (uint32_t)__cvta_generic_to_shared(s_tri);
+		if (threadIdx.x == 0) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+			asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+			asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+			asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+			             "l"(src), "r"(bytes), "r"(bar)
+			             : "memory");
+		}
+		__syncthreads();
+		if (!mbar_wait(bar, 0)) {
+			set_error(L, kErrBulkTimeout);
+			for (uint32_t i = threadIdx.x; i < cnt * 9u; i += blockDim.x) s_tri[i] = src[i];
+		}
+	} else {
+		for (uint32_t i = threadIdx.x; i < cnt * 9u; i += blockDim.x) s_tri[i] = src[i];
+	}
+	__syncthreads();
+}
+
+template <class P>
+__global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_cols) {
+	__shared__ __align__(16) float s_tri[kTile * 9];
+	__shared__ __align__(8) uint64_t s_bar;
+	const uint32_t tile = blockIdx.x;
+	const uint32_t j = job_of_tile(L, tile);
+	const JobDesc& J = job_at(L, j);
+	const uint64_t n = J.n_tri;
+	const bool morton = (J.flags & JOB_MORTON) != 0;
+	const float bmin[3] = {J.bmin[0], J.bmin[1], J.bmin[2]};
+	const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
+	const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
+	uint32_t* flips = J.flips;
+	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
+	const uint32_t cnt = (uint32_t)umin64((uint64_t)kTile, n - t0);
+	stage_tile(L, J.tris + t0 * 9, cnt, s_tri, &s_bar);
+
+	const uint32_t lane = threadIdx.x & 31u;
+	bool is_mid = false, is_big = false;
+	uint32_t n_items = 0;
+	if (threadIdx.x < cnt) {
+		float t[9];
+#pragma unroll
+		for (int k = 0; k < 9; k++) t[k] = s_tri[threadIdx.x * 9 + k];
+		SolidTri S;
+		solid_setup<P>(t, bmin, unit, grid, S);
+		if (!S.skip && S.y0 <= S.y1 && S.z0 <= S.z1) {
+			const uint64_t ncols = (uint64_t)(S.y1 - S.y0 + 1) * (uint64_t)(S.z1 - S.z0 + 1);
+			if (ncols <= small_cols) {
+				for (int y = S.y0; y <= S.y1; y++)
+					for (int z = S.z0; z <= S.z1; z++) {
+						int xmax;
+						if (column_hit<P>(S, unit, y, z, xmax)) record_hit(flips, grid, morton, y, z, xmax);
+					}
+			} else {
+				const uint64_t it = (ncols + kColsPerItem - 1) / kColsPerItem;
+				n_items = (uint32_t)umin64(it, 0xFFFFFFu);
+				is_mid = n_items == 1;
+				is_big = n_items > 1;
+			}
+		}
+	}
+	const uint32_t lt = (1u << lane) - 1u;
+	const uint32_t mid_ballot = __ballot_sync(FULL, is_mid);
+	if (mid_ballot) {
+		uint32_t base = 0;
+		const uint32_t leader = __ffs(mid_ballot) - 1;
+		if (lane == leader) base = atomicAdd(&L.scr.ctr->mid, (unsigned)__popc(mid_ballot));
+		base = __shfl_sync(FULL, base, leader);
+		const uint32_t slot = base + __popc(mid_ballot & lt);
+		if (is_mid) {
+			if (slot < L.scr.cap) L.scr.mid[slot] = MidRec{j, (uint32_t)(t0 + threadIdx.x)};
+			else set_error(L, kErrQueueOverflow);
+		}
+	}
+	const uint32_t big_ballot = __ballot_sync(FULL, is_big);
+	if (big_ballot) {
+		uint32_t incl = is_big ? n_items : 0u;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t v = __shfl_up_sync(FULL, incl, d);
+			if (lane >= (uint32_t)d) incl += v;
+		}
+		const uint32_t total = __shfl_sync(FULL, incl, 31);
+		unsigned long long old = 0;
+		if (lane == 0)
+			old = atomicAdd(&L.scr.ctr->big, ((unsigned long long)__popc(big_ballot) << kBigShift) | (unsigned long long)total);
+		old = __shfl_sync(FULL, old, 0);
+		if (is_big) {
+			const uint32_t rec = (uint32_t)(old >> kBigShift) + __popc(big_ballot & lt);
+			const uint64_t first = (old & kBigItemMask) + incl - n_items;
+			if (rec < L.scr.cap && first + n_items <= kBigItemMask)
+				L.scr.big[rec] = BigRec{first, j, (uint32_t)(t0 + threadIdx.x), n_items, 0u};
+			else
+				set_error(L, kErrQueueOverflow);
+		}
+	}
+}
+
+template <class P>
+__global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant__ LaunchDesc L) {
+	const uint32_t lane = threadIdx.x & 31u;
+	Counters* C = L.scr.ctr;
+	const unsigned long long bigc = *reinterpret_cast<volatile unsigned long long*>(&C->big);
+	const uint32_t n_big = min((uint32_t)(bigc >> kBigShift), L.scr.cap);
+	const uint64_t n_big_items = bigc & kBigItemMask;
+	const uint32_t n_mid = min(*reinterpret_cast<volatile unsigned*>(&C->mid), L.scr.cap);
+	const uint64_t total = n_big_items + n_mid;
+	for (;;) {
+		unsigned long long tk = 0;
+		if (lane == 0) tk = atomicAdd(&C->ticket, 1ull);
+		tk = __shfl_sync(FULL, tk, 0);
+		if (tk >= total) break;
+		uint32_t job = 0, tri = 0, chunk = 0, ok = 0;
+		if (lane == 0) {
+			if (tk < n_big_items) {
+				if (n_big > 0) {
+					uint32_t lo = 0, hi = n_big - 1;
+					while (lo < hi) {
+						const uint32_t m = (lo + hi + 1) >> 1;
+						if (L.scr.big[m].item_begin <= tk) lo = m; else hi = m - 1;
+					}
+					const BigRec r = L.scr.big[lo];
+					job = r.job; tri = r.tri; chunk = (uint32_t)(tk - r.item_begin);
+					ok = tk >= r.item_begin && chunk < r.n_items;
+				}
+			} else {
+				const MidRec r = L.scr.mid[tk - n_big_items];
+				job = r.job; tri = r.tri;
+				ok = 1;
+			}
+			// never follow a malformed record (only possible after a queue overflow)
+			if (ok && (job >= L.n_jobs || tri >= job_at(L, job).n_tri)) ok = 0;
+		}
+		ok = __shfl_sync(FULL, ok, 0);
+		if (!ok) continue;
+		job = __shfl_sync(FULL, job, 0);
+		tri = __shfl_sync(FULL, tri, 0);
+		chunk = __shfl_sync(FULL, chunk, 0);
+		const JobDesc& J = job_at(L, job);
+		const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
+		const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
+		const bool morton = (J.flags & JOB_MORTON) != 0;
+		float tv = lane < 9 ? J.tris[(uint64_t)tri * 9 + lane] : 0.0f;
+		float t[9];
+#pragma unroll
+		for (int k = 0; k < 9; k++) t[k] = __shfl_sync(FULL, tv, k);
+		SolidTri S;
+		solid_setup<P>(t, J.bmin, unit, grid, S);
+		const uint64_t nzc = (uint64_t)(S.z1 - S.z0 + 1);
+		const uint64_t ncols = (uint64_t)(S.y1 - S.y0 + 1) * nzc;
+		const uint64_t c0 = (uint64_t)chunk * kColsPerItem;
+		const uint64_t c1 = umin64(ncols, c0 + kColsPerItem);
+		for (uint64_t c = c0 + lane; c < c1; c += 32) {
+			const int y = S.y0 + (int)(c / nzc), z = S.z0 + (int)(c % nzc);
+			int xmax;
+			if (column_hit<P>(S, unit, y, z, xmax)) record_hit(J.flips, grid, morton, y, z, xmax);
+		}
+	}
+}
+
+__device__ __forceinline__ uint32_t prefix_xor_msb(uint32_t t) {
+	t ^= t >> 1;
+	t ^= t >> 2;
+	t ^= t >> 4;
+	t ^= t >> 8;
+	t ^= t >> 16;
+	return t;
+}
+
+// One warp per resolve unit.  A unit is a run of whole rows starting on a word boundary.
+__global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ LaunchDesc L) {
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t unit_id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	if (unit_id >= L.n_units) return;
+	const uint32_t j = job_search(L, unit_id, [](const JobDesc& d) { return (uint64_t)d.unit_begin; });
+	const JobDesc& J = job_at(L, j);
+	const uint64_t gx = J.grid[0];
+	const uint64_t rows = (uint64_t)J.grid[1] * J.grid[2];
+	const bool morton = (J.flags & JOB_MORTON) != 0;
+	uint32_t* flips = J.flips;
+	uint32_t* dest = J.table;
+	const uint64_t u = unit_id - J.unit_begin;
+	if (gx % 32 == 0) {
+		const uint64_t wpr = gx >> 5;
+		const uint64_t rpu = wpr >= 1024 ? 1 : 1024 / wpr;
+		const uint64_t r0 = u * rpu, r1 = min(rows, r0 + rpu);
+		const uint64_t wbeg = r0 * wpr, wend = r1 * wpr;
+		uint32_t carry = 0;
+		for (uint64_t wb = wbeg; wb < wend; wb += 32) {
+			const uint64_t w = wb + lane;
+			const bool active = w < wend;
+			const uint32_t t = active ? flips[w] : 0u;
+			const uint32_t x = __popc(t) & 1u;
+			uint32_t v = x;
+			bool f = active && ((w - wbeg) % wpr == 0);
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				const uint32_t uv = __shfl_up_sync(FULL, v, d);
+				const bool uf = __shfl_up_sync(FULL, (int)f, d) != 0;
+				if (lane >= (uint32_t)d) {
+					if (!f) v ^= uv;
+					f = f || uf;
+				}
+			}
+			const uint32_t vin = f ? v : (v ^ carry);
+			const uint32_t res = prefix_xor_msb(t) ^ ((vin ^ x) ? 0xFFFFFFFFu : 0u);
+			if (active) {
+				if (morton) {
+					flips[w] = res;
+				} else {
+					if (res) dest[w] ^= res;
+					if (t) flips[w] = 0u;
+				}
+			}
+			carry = __shfl_sync(FULL, vin, 31);
+		}
+	} else if (lane == 0) {
+		// Rows not word aligned: walk the unit's bits serially (odd grid sizes only).
+		const uint64_t g = gx;
+		uint64_t p = 32;  // lcm(gx, 32) / gx rows per unit
+		{
+			uint64_t a = g, b = 32;
+			while (b) { uint64_t r = a % b; a = b; b = r; }
+			p = 32 / a;
+		}
+		const uint64_t r0 = u * p, r1 = min(rows, r0 + p);
+		const uint64_t b0 = r0 * g, b1 = r1 * g;
+		uint32_t carry = 0;
+		for (uint64_t w = b0 >> 5; (w << 5) < b1; w++) {
+			const uint32_t t = flips[w];
+			uint32_t res = 0;
+			for (uint32_t k = 0; k < 32; k++) {
+				const uint64_t b = (w << 5) + k;
+				if (b >= b1) break;
+				if (b % g == 0) carry = 0;
+				carry ^= (t >> (31 - k)) & 1u;
+				res |= carry << (31 - k);
+			}
+			if (morton) {
+				flips[w] = res;
+			} else {
+				if (res) dest[w] ^= res;
+				if (t) flips[w] = 0u;
+			}
+		}
+	}
+}
+
+__device__ __forceinline__ uint32_t compact3(uint64_t v) {
+	v &= 0x249249249249ull;
+	v = (v ^ (v >> 2)) & 0x0C30C30C30C3ull;
+	v = (v ^ (v >> 4)) & 0x00F00F00F00Full;
+	v = (v ^ (v >> 8)) & 0x0000FF0000FFull;
+	v = (v ^ (v >> 16)) & 0xFFFFull;
+	return (uint32_t)v;
+}
+
+// Morton jobs: XOR the resolved linear bits into Morton order, one Morton word per thread.
+__global__ void __launch_bounds__(256) solid_morton(const __grid_constant__ LaunchDesc L) {
+	const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (idx >= L.n_mwords) return;
+	const uint32_t j = job_search(L, idx, [](const JobDesc& d) { return d.mword_begin; });
+	const JobDesc& J = job_at(L, j);
+	const uint64_t m = idx - J.mword_begin;
+	const uint64_t g = J.grid[0];
+	const uint32_t* flips = J.flips;
+	uint32_t out = 0;
+	if (g >= 32) {
+		// the word holds a 4x4x2 brick: x = 4X+dx, y = 4Y+dy, z = 2Z+dz
+		const uint64_t X = compact3(m >> 1), Y = compact3(m >> 2), Z = compact3(m);
+		const uint64_t x0 = 4 * X;
+#pragma unroll
+		for (uint32_t dz = 0; dz < 2; dz++)
+#pragma unroll
+			for (uint32_t dy = 0; dy < 4; dy++) {
+				const uint64_t row = (2 * Z + dz) * g + (4 * Y + dy);
+				const uint64_t lin = row * g + x0;
+				const uint32_t nib = (flips[lin >> 5] >> (28u - (uint32_t)(lin & 31u))) & 0xFu;
+#pragma unroll
+				for (uint32_t dx = 0; dx < 4; dx++) {
+					const uint32_t o = (dx & 1u) | ((dy & 1u) << 1) | (dz << 2) | ((dx >> 1) << 3) | ((dy >> 1) << 4);
+					out |= ((nib >> (3u - dx)) & 1u) << (31u - o);
+				}
+			}
+	} else {
+		const uint64_t total = g * g * g;
+		for (uint32_t i = 0; i < 32; i++) {
+			const uint64_t c = m * 32 + i;
+			if (c >= total) break;
+			const uint64_t x = compact3(c), y = compact3(c >> 1), z = compact3(c >> 2);
+			const uint64_t lin = x + g * (y + g * z);
+			out |= ((flips[lin >> 5] >> (31u - (uint32_t)(lin & 31u))) & 1u) << (31u - i);
+		}
+	}
+	if (out) J.table[m] ^= out;
+}
+
+// Morton jobs: clear the resolved flip table, one warp per resolve unit.
+__global__ void __launch_bounds__(256) solid_zero(const __grid_constant__ LaunchDesc L) {
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t unit_id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	if (unit_id >= L.n_units) return;
+	const uint32_t j = job_search(L, unit_id, [](const JobDesc& d) { return (uint64_t)d.unit_begin; });
+	const JobDesc& J = job_at(L, j);
+	if (!(J.flags & JOB_MORTON)) return;
+	const uint64_t gx = J.grid[0];
+	const uint64_t rows = (uint64_t)J.grid[1] * J.grid[2];
+	uint64_t rpu;
+	if (gx % 32 == 0) {
+		const uint64_t wpr = gx >> 5;
+		rpu = wpr >= 1024 ? 1 : 1024 / wpr;
+	} else {
+		uint64_t a = gx, b = 32;
+		while (b) { uint64_t r = a % b; a = b; b = r; }
+		rpu = 32 / a;
+	}
+	const uint64_t u = unit_id - J.unit_begin;
+	const uint64_t r0 = u * rpu, r1 = min(rows, r0 + rpu);
+	const uint64_t wbeg = (r0 * gx) >> 5, wend = (r1 * gx + 31) >> 5;
+	for (uint64_t w = wbeg + lane; w < wend; w += 32) J.flips[w] = 0u;
+}
+
+}  // namespace
+
+SolidUnits solid_units(const uint32_t grid[3]) {
+	const uint64_t gx = grid[0];
+	const uint64_t rows = (uint64_t)grid[1] * grid[2];
+	SolidUnits s;
+	s.aligned = gx % 32 == 0;
+	if (s.aligned) {
+		const uint64_t wpr = gx >> 5;
+		s.rows_per_unit = wpr >= 1024 ? 1 : 1024 / wpr;
+	} else {
+		uint64_t a = gx, b = 32;
+		while (b) { uint64_t r = a % b; a = b; b = r; }
+		s.rows_per_unit = 32 / a;
+	}
+	s.units = (rows + s.rows_per_unit - 1) / s.rows_per_unit;
+	return s;
+}
+
+template <class P>
+static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases) {
+	cudaError_t e = cudaSuccess;
+	if ((phases & kSolidToggles) && L.n_tiles) {
+		solid_classify<P><<<L.n_tiles, kTile, 0, s>>>(L, tune.small_cols);
+		if ((e = cudaGetLastError()) != cudaSuccess) return e;
+		solid_cols<P><<<cols_grid, kRowsThreads, 0, s>>>(L);
+		if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	}
+	if (phases & kSolidResolve) {
+		if (L.n_units) {
+			solid_resolve<<<(L.n_units + 7) / 8, 256, 0, s>>>(L);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+		}
+		if (L.n_mwords) {
+			solid_morton<<<(unsigned)((L.n_mwords + 255) / 256), 256, 0, s>>>(L);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			solid_zero<<<(L.n_units + 7) / 8, 256, 0, s>>>(L);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+		}
+	}
+	return cudaSuccess;
+}
+
+cudaError_t launch_solid(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases) {
+	return launch_solid_t<RefFma>(L, tune, cols_grid, s, phases);
+}
+
+int solid_cols_blocks_per_sm() {
+	int n = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, solid_cols<RefFma>, kRowsThreads, 0);
+	return n > 0 ? n : 1;
+}
+
+}  // namespace cvx

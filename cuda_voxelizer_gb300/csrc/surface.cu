@@ -1,0 +1,303 @@
+// surface.cu -- surface voxelization kernels (reference: voxelize_triangle, src/voxelize.cu:58-190).
+//
+// Two kernels per launch sequence, both over a job table so that one mesh and a batch of meshes
+// run through the same code:
+//   surf_classify  one CTA per tile of 256 triangles of one job.  The tile is staged into shared
+//                  memory with one cp.async.bulk (TMA bulk copy) when it is full and 16-byte
+//                  aligned.  Each thread sets up its triangle; triangles whose grid bbox holds at
+//                  most `small_vox` voxels are finished in the thread (every voxel of the bbox
+//                  tested, like the reference); the others are queued, one record per triangle,
+//                  as one item ("mid") or as one item per 32 z-slices ("big").
+//   surf_rows      persistent CTAs; each warp takes work tickets (big items first, then mid
+//                  triangles), finds the y-interval of every z-slice of the item (one lane per
+//                  slice), flattens the (y, z) rows and gives one row per lane; each lane finds the
+//                  exact x-interval of its row and ORs it into the table one word at a time.
+#include "engine.h"
+#include "surface.cuh"
+
+namespace cvx {
+
+namespace {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+// Bounded wait on an mbarrier phase.  Returns false if the phase did not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+	for (uint32_t it = 0; it < (1u << 24); it++) {
+		uint32_t ok;
+		asm volatile(
+		    "{\n\t.reg .pred p;\n\t"
+		    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+		    "selp.u32 %0, 1, 0, p;\n\t}"
+		    : "=r"(ok)
+		    : "r"(bar), "r"(parity)
+		    : "memory");
+		if (ok) return true;
+	}
+	return false;
+}
+
+// Stage `cnt` triangles (9 floats each) from global memory into shared memory.  A full, aligned
+// tile goes through one bulk copy completing on an mbarrier; anything else is loaded cooperatively.
+__device__ __forceinline__ void stage_tile(const LaunchDesc& L, const float* src, uint32_t cnt, float* s_tri,
+                                           uint64_t* s_bar) {
+	const uint32_t bytes = cnt * 36u;
+	const bool bulk = cnt == kTile && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0);
+	if (bulk) {
+		const uint32_t bar = (uint32_t)__cvta_generic_to_shared(s_bar);
+		const uint32_t dst = (uint32_t)__cvta_generic_to_shared(s_tri);
+		if (threadIdx.x == 0) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+			asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+			asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+			asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+			             "l"(src), "r"(bytes), "r"(bar)
+			             : "memory");
+		}
+		__syncthreads();  // barrier initialised before anyone waits on it
+		if (!mbar_wait(bar, 0)) {
+			// The copy did not land in time: flag it and read the tile directly instead.  The
+			// bulk copy writes the same bytes whenever it completes.
+			set_error(L, kErrBulkTimeout);
+			for (uint32_t i = threadIdx.x; i < cnt * 9u; i += blockDim.x) s_tri[i] = src[i];
+		}
+	} else {
+		for (uint32_t i = threadIdx.x; i < cnt * 9u; i += blockDim.x) s_tri[i] = src[i];
+	}
+	__syncthreads();
+}
+
+// Accumulates bits of consecutive voxels that share a table word, one atomicOr per word.
+struct WordSink {
+	uint32_t* table;
+	uint64_t word = ~0ull;
+	uint32_t mask = 0;
+	__device__ __forceinline__ void add(uint64_t idx) {
+		const uint64_t w = idx >> 5;
+		if (w != word) {
+			if (mask) atomicOr(table + word, mask);
+			word = w;
+			mask = 0;
+		}
+		mask |= bit_of(idx);
+	}
+	__device__ __forceinline__ void flush() {
+		if (mask) atomicOr(table + word, mask);
+		mask = 0;
+	}
+};
+
+template <class P>
+__global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_vox) {
+	__shared__ __align__(16) float s_tri[kTile * 9];
+	__shared__ __align__(8) uint64_t s_bar;
+	const uint32_t tile = blockIdx.x;
+	const uint32_t j = job_of_tile(L, tile);
+	const JobDesc& J = job_at(L, j);
+	const float* tris = J.tris;
+	uint32_t* table = J.table;
+	const uint64_t n = J.n_tri;
+	const bool morton = (J.flags & JOB_MORTON) != 0;
+	const float bmin[3] = {J.bmin[0], J.bmin[1], J.bmin[2]};
+	const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
+	const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
+	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
+	const uint32_t cnt = (uint32_t)umin64((uint64_t)kTile, n - t0);
+	stage_tile(L, tris + t0 * 9, cnt, s_tri, &s_bar);
+
+	const uint32_t lane = threadIdx.x & 31u;
+	const bool valid = threadIdx.x < cnt;
+	bool is_mid = false, is_big = false;
+	uint32_t n_items = 0;
+	if (valid) {
+		float t[9];
+#pragma unroll
+		for (int k = 0; k < 9; k++) t[k] = s_tri[threadIdx.x * 9 + k];
+		SurfTri S;
+		surf_setup<P>(t, bmin, unit, grid, S);
+		const uint64_t nvox = (uint64_t)(S.bx1 - S.bx0 + 1) * (uint64_t)(S.by1 - S.by0 + 1) * (uint64_t)(S.bz1 - S.bz0 + 1);
+		if (nvox <= small_vox) {
+			// Small triangle: test every voxel of its bbox (src/voxelize.cu:136-183).
+			WordSink sink{table};
+			for (int z = S.bz0; z <= S.bz1; z++) {
+				const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
+				for (int y = S.by0; y <= S.by1; y++) {
+					const float py = __fmul_rn(__int2float_rn(y), unit[1]);
+					if (yz_fail_bits<P>(S, py, pz)) continue;
+					RowK K;
+					row_consts<P>(S, py, pz, K);
+					const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
+					const uint64_t yzm = morton ? ((spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2)) : 0;
+					for (int x = S.bx0; x <= S.bx1; x++) {
+						if (fail_bits<P>(S, K, unit[0], x)) continue;
+						sink.add(morton ? (spread3((uint32_t)x) | yzm) : base + (uint64_t)x);
+					}
+				}
+			}
+			sink.flush();
+		} else {
+			n_items = (uint32_t)((S.bz1 - S.bz0 + kZch) / kZch);
+			is_mid = n_items == 1;
+			is_big = n_items > 1;
+		}
+	}
+	// Queue the remaining triangles: warp-aggregated appends.
+	const uint32_t lt = (1u << lane) - 1u;
+	const uint32_t mid_ballot = __ballot_sync(FULL, is_mid);
+	if (mid_ballot) {
+		uint32_t base = 0;
+		const uint32_t leader = __ffs(mid_ballot) - 1;
+		if (lane == leader) base = atomicAdd(&L.scr.ctr->mid, (unsigned)__popc(mid_ballot));
+		base = __shfl_sync(FULL, base, leader);
+		const uint32_t slot = base + __popc(mid_ballot & lt);
+		if (is_mid) {
+			if (slot < L.scr.cap) L.scr.mid[slot] = MidRec{j, (uint32_t)(t0 + threadIdx.x)};
+			else set_error(L, kErrQueueOverflow);
+		}
+	}
+	const uint32_t big_ballot = __ballot_sync(FULL, is_big);
+	if (big_ballot) {
+		uint32_t incl = is_big ? n_items : 0u;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t v = __shfl_up_sync(FULL, incl, d);
+			if (lane >= (uint32_t)d) incl += v;
+		}
+		const uint32_t total = __shfl_sync(FULL, incl, 31);
+		unsigned long long old = 0;
+		if (lane == 0)
+			old = atomicAdd(&L.scr.ctr->big, ((unsigned long long)__popc(big_ballot) << kBigShift) | (unsigned long long)total);
+		old = __shfl_sync(FULL, old, 0);
+		if (is_big) {
+			const uint32_t rec = (uint32_t)(old >> kBigShift) + __popc(big_ballot & lt);
+			const uint64_t first = (old & kBigItemMask) + incl - n_items;
+			if (rec < L.scr.cap && first + n_items <= kBigItemMask)
+				L.scr.big[rec] = BigRec{first, j, (uint32_t)(t0 + threadIdx.x), n_items, 0u};
+			else
+				set_error(L, kErrQueueOverflow);
+		}
+	}
+}
+
+template <class P>
+__global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant__ LaunchDesc L) {
+	const uint32_t lane = threadIdx.x & 31u;
+	Counters* C = L.scr.ctr;
+	const unsigned long long bigc = *reinterpret_cast<volatile unsigned long long*>(&C->big);
+	const uint32_t n_big = min((uint32_t)(bigc >> kBigShift), L.scr.cap);
+	const uint64_t n_big_items = bigc & kBigItemMask;
+	const uint32_t n_mid = min(*reinterpret_cast<volatile unsigned*>(&C->mid), L.scr.cap);
+	const uint64_t total = n_big_items + n_mid;
+	for (;;) {
+		unsigned long long tk = 0;
+		if (lane == 0) tk = atomicAdd(&C->ticket, 1ull);
+		tk = __shfl_sync(FULL, tk, 0);
+		if (tk >= total) break;
+		uint32_t job = 0, tri = 0, chunk = 0, ok = 0;
+		if (lane == 0) {
+			if (tk < n_big_items) {
+				if (n_big > 0) {
+					uint32_t lo = 0, hi = n_big - 1;
+					while (lo < hi) {
+						const uint32_t m = (lo + hi + 1) >> 1;
+						if (L.scr.big[m].item_begin <= tk) lo = m; else hi = m - 1;
+					}
+					const BigRec r = L.scr.big[lo];
+					job = r.job; tri = r.tri; chunk = (uint32_t)(tk - r.item_begin);
+					ok = tk >= r.item_begin && chunk < r.n_items;
+				}
+			} else {
+				const MidRec r = L.scr.mid[tk - n_big_items];
+				job = r.job; tri = r.tri;
+				ok = 1;
+			}
+			// never follow a malformed record (only possible after a queue overflow)
+			if (ok && (job >= L.n_jobs || tri >= job_at(L, job).n_tri)) ok = 0;
+		}
+		ok = __shfl_sync(FULL, ok, 0);
+		if (!ok) continue;
+		job = __shfl_sync(FULL, job, 0);
+		tri = __shfl_sync(FULL, tri, 0);
+		chunk = __shfl_sync(FULL, chunk, 0);
+		const JobDesc& J = job_at(L, job);
+		const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
+		const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
+		const bool morton = (J.flags & JOB_MORTON) != 0;
+		uint32_t* table = J.table;
+		float tv = lane < 9 ? J.tris[(uint64_t)tri * 9 + lane] : 0.0f;
+		float t[9];
+#pragma unroll
+		for (int k = 0; k < 9; k++) t[k] = __shfl_sync(FULL, tv, k);
+		SurfTri S;
+		surf_setup<P>(t, J.bmin, unit, grid, S);
+		RowDirs D;
+		row_dirs(S, unit[0], D);
+
+		// y-interval of this lane's z-slice
+		const int z0 = S.bz0 + (int)(chunk * kZch);
+		const int zl = z0 + (int)lane;
+		int ya = 0, yb = -1;
+		if (zl <= S.bz1) {
+			const float pz = __fmul_rn(__int2float_rn(zl), unit[2]);
+			if (!y_interval<P>(S, unit[1], pz, ya, yb)) { ya = 0; yb = -1; }
+		}
+		const int cnt = yb - ya + 1;
+		int incl = cnt;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const int v = __shfl_up_sync(FULL, incl, d);
+			if (lane >= (uint32_t)d) incl += v;
+		}
+		const int R = __shfl_sync(FULL, incl, 31);
+		for (int base = 0; base < R; base += 32) {
+			const int k = base + (int)lane;
+			// slice s = first lane whose inclusive count exceeds k
+			int s = 0;
+#pragma unroll
+			for (int step = 16; step >= 1; step >>= 1) {
+				const int v = __shfl_sync(FULL, incl, s + step - 1);
+				if (v <= k) s += step;
+			}
+			s = min(s, 31);
+			const int incl_s = __shfl_sync(FULL, incl, s);
+			const int cnt_s = __shfl_sync(FULL, cnt, s);
+			const int ya_s = __shfl_sync(FULL, ya, s);
+			if (k < R) {
+				const int y = ya_s + (k - (incl_s - cnt_s));
+				const int z = z0 + s;
+				const float py = __fmul_rn(__int2float_rn(y), unit[1]);
+				const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
+				RowK K;
+				row_consts<P>(S, py, pz, K);
+				int xl, xh;
+				if (row_interval<P>(S, D, K, unit[0], xl, xh)) write_row(table, morton, grid, y, z, xl, xh);
+			}
+		}
+	}
+}
+
+}  // namespace
+
+// ---- host-side launchers ------------------------------------------------------------------------
+
+template <class P>
+static cudaError_t launch_surface_t(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s) {
+	if (L.n_tiles == 0) return cudaSuccess;
+	surf_classify<P><<<L.n_tiles, kTile, 0, s>>>(L, tune.small_vox);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	surf_rows<P><<<rows_grid, kRowsThreads, 0, s>>>(L);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s) {
+	return launch_surface_t<RefFma>(L, tune, rows_grid, s);
+}
+
+int surf_rows_blocks_per_sm() {
+	int n = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, surf_rows<RefFma>, kRowsThreads, 0);
+	return n > 0 ? n : 1;
+}
+
+}  // namespace cvx

@@ -1,0 +1,279 @@
+// surface.cuh -- exact surface-voxelization predicates (Schwarz-Seidel triangle/box overlap) and
+// the row-interval search built on them.
+//
+// Reference: voxelize_triangle, src/voxelize.cu:58-190.  Per triangle the reference computes a
+// plane test (:89-95) and nine 2D edge functions (:97-133) once, then tests every voxel of the
+// triangle's grid bbox (:136-181).  Here the per-triangle part is SurfTri/surf_setup; the per-voxel
+// part is fail_bits + yz_pass, which evaluate the very same fp32 expressions for a voxel (x, y, z).
+//
+// Row intervals.  For a fixed row (y, z) every test depends on x only through p.x = x * unit.x,
+// and each test value is a composition of correctly rounded, monotone operations of p.x.  So each
+// edge test passes on a prefix or a suffix of x, and so does each side of the plane test (see
+// fail_bits).  The voxels of a row that pass all tests therefore form one interval [xl, xh].
+// row_interval finds it: a real-valued estimate of every test's crossing picks the candidate
+// ends, then exact evaluations at the candidates (and a walk if an estimate was off) pin them.
+// The result is identical to testing every voxel of the row; only the number of evaluations
+// changes.
+#pragma once
+#include "cvx_device.cuh"
+
+namespace cvx {
+
+struct SurfTri {
+	float nx, ny, nz, d1, d2;
+	float exy[3][2], eyz[3][2], ezx[3][2];   // edge normals n_xy_ei, n_yz_ei, n_zx_ei after the flips
+	float dxy[3], dyz[3], dzx[3];
+	int bx0, by0, bz0, bx1, by1, bz1;        // clamped grid bbox
+};
+
+// Triangle setup, src/voxelize.cu:71-133.  `t` holds v0.xyz, v1.xyz, v2.xyz in world space.
+template <class P>
+__device__ __forceinline__ void surf_setup(const float* t, const float* bmin, const float* unit, const uint32_t* grid,
+                                           SurfTri& S) {
+	const float v0x = __fsub_rn(t[0], bmin[0]), v0y = __fsub_rn(t[1], bmin[1]), v0z = __fsub_rn(t[2], bmin[2]);
+	const float v1x = __fsub_rn(t[3], bmin[0]), v1y = __fsub_rn(t[4], bmin[1]), v1z = __fsub_rn(t[5], bmin[2]);
+	const float v2x = __fsub_rn(t[6], bmin[0]), v2y = __fsub_rn(t[7], bmin[1]), v2z = __fsub_rn(t[8], bmin[2]);
+	const float e0x = __fsub_rn(v1x, v0x), e0y = __fsub_rn(v1y, v0y), e0z = __fsub_rn(v1z, v0z);
+	const float e1x = __fsub_rn(v2x, v1x), e1y = __fsub_rn(v2y, v1y), e1z = __fsub_rn(v2z, v1z);
+	const float e2x = __fsub_rn(v0x, v2x), e2y = __fsub_rn(v0y, v2y), e2z = __fsub_rn(v0z, v2z);
+	// n = normalize(cross(e0, e1))  (helper_math cross / normalize: v * rsqrtf(dot(v, v)))
+	const float cx = mul_sub<P::cross>(e0y, e1z, e0z, e1y);
+	const float cy = mul_sub<P::cross>(e0z, e1x, e0x, e1z);
+	const float cz = mul_sub<P::cross>(e0x, e1y, e0y, e1x);
+	const float inv = rsqrtf(dot3<P::dot3>(cx, cy, cz, cx, cy, cz));
+	S.nx = __fmul_rn(cx, inv);
+	S.ny = __fmul_rn(cy, inv);
+	S.nz = __fmul_rn(cz, inv);
+
+	// grid bbox: clamp(int(min(v) / unit), 0, g - 1)  (:83-87)
+	const int gmx = (int)grid[0] - 1, gmy = (int)grid[1] - 1, gmz = (int)grid[2] - 1;
+	S.bx0 = min(max(__float2int_rz(__fdiv_rn(fminf(v0x, fminf(v1x, v2x)), unit[0])), 0), gmx);
+	S.by0 = min(max(__float2int_rz(__fdiv_rn(fminf(v0y, fminf(v1y, v2y)), unit[1])), 0), gmy);
+	S.bz0 = min(max(__float2int_rz(__fdiv_rn(fminf(v0z, fminf(v1z, v2z)), unit[2])), 0), gmz);
+	S.bx1 = min(max(__float2int_rz(__fdiv_rn(fmaxf(v0x, fmaxf(v1x, v2x)), unit[0])), 0), gmx);
+	S.by1 = min(max(__float2int_rz(__fdiv_rn(fmaxf(v0y, fmaxf(v1y, v2y)), unit[1])), 0), gmy);
+	S.bz1 = min(max(__float2int_rz(__fdiv_rn(fmaxf(v0z, fmaxf(v1z, v2z)), unit[2])), 0), gmz);
+
+	// plane test: critical point c and d1, d2  (:90-95)
+	const float cxp = S.nx > 0.0f ? unit[0] : 0.0f;
+	const float cyp = S.ny > 0.0f ? unit[1] : 0.0f;
+	const float czp = S.nz > 0.0f ? unit[2] : 0.0f;
+	S.d1 = dot3<P::dot3>(S.nx, S.ny, S.nz, __fsub_rn(cxp, v0x), __fsub_rn(cyp, v0y), __fsub_rn(czp, v0z));
+	S.d2 = dot3<P::dot3>(S.nx, S.ny, S.nz, __fsub_rn(__fsub_rn(unit[0], cxp), v0x),
+	                     __fsub_rn(__fsub_rn(unit[1], cyp), v0y), __fsub_rn(__fsub_rn(unit[2], czp), v0z));
+
+	// projection tests (:97-133).  n_xy_e = (-e.y, e.x), negated when n.z < 0; d = -dot(n_e, v) +
+	// max(0, u.a * n_e.x) + max(0, u.b * n_e.y).
+	const float ex[3] = {e0x, e1x, e2x}, ey[3] = {e0y, e1y, e2y}, ez[3] = {e0z, e1z, e2z};
+	const float vx[3] = {v0x, v1x, v2x}, vy[3] = {v0y, v1y, v2y}, vz[3] = {v0z, v1z, v2z};
+	const float sxy = S.nz < 0.0f ? -1.0f : 1.0f;
+	const float syz = S.nx < 0.0f ? -1.0f : 1.0f;
+	const float szx = S.ny < 0.0f ? -1.0f : 1.0f;
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		// -1.0f * e.y and the sign flips are exact negations
+		const float axy = sxy * -ey[i], bxy = sxy * ex[i];
+		const float ayz = syz * -ez[i], byz = syz * ey[i];
+		const float azx = szx * -ex[i], bzx = szx * ez[i];
+		S.exy[i][0] = axy; S.exy[i][1] = bxy;
+		S.eyz[i][0] = ayz; S.eyz[i][1] = byz;
+		S.ezx[i][0] = azx; S.ezx[i][1] = bzx;
+		S.dxy[i] = __fadd_rn(__fadd_rn(-mul_add<P::dot2>(axy, vx[i], bxy, vy[i]), fmaxf(0.0f, __fmul_rn(unit[0], axy))),
+		                     fmaxf(0.0f, __fmul_rn(unit[1], bxy)));
+		S.dyz[i] = __fadd_rn(__fadd_rn(-mul_add<P::dot2>(ayz, vy[i], byz, vz[i]), fmaxf(0.0f, __fmul_rn(unit[1], ayz))),
+		                     fmaxf(0.0f, __fmul_rn(unit[2], byz)));
+		S.dzx[i] = __fadd_rn(__fadd_rn(-mul_add<P::dot2>(azx, vz[i], bzx, vx[i]), fmaxf(0.0f, __fmul_rn(unit[0], azx))),
+		                     fmaxf(0.0f, __fmul_rn(unit[2], bzx)));
+	}
+}
+
+// Per-row constants of the x-dependent tests (products that do not involve p.x).
+struct RowK {
+	float py, pz;
+	float kpl;       // plane: ny*py (pattern 1) / the partial sum the pattern keeps fixed
+	float kpl2;      // plane: nz*pz (pattern 2)
+	float kxy[3];    // XY edge i: n_xy.y * p.y (pattern 1)
+	float kzx[3];    // ZX edge i: n_zx.x * p.z (pattern 2)
+};
+
+template <class P>
+__device__ __forceinline__ void row_consts(const SurfTri& S, float py, float pz, RowK& K) {
+	K.py = py;
+	K.pz = pz;
+	K.kpl = (P::plane == 3) ? 0.0f : __fmul_rn(S.ny, py);
+	K.kpl2 = __fmul_rn(S.nz, pz);
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		K.kxy[i] = __fmul_rn(S.exy[i][1], py);
+		K.kzx[i] = __fmul_rn(S.ezx[i][0], pz);
+	}
+}
+
+// Bit i set = x-dependent test i fails at voxel x of the row.
+//   bit 0: plane test fails with both (s+d1), (s+d2) < 0   ("below" the slab)
+//   bit 1: plane test fails with both > 0                  ("above")
+//   bits 2-4: XY edge tests, bits 5-7: ZX edge tests.
+// The reference fails the plane test iff (s+d1)*(s+d2) > 0 (:146); a positive product needs equal
+// signs, so bit0|bit1 is exactly that condition.  As x grows, s moves monotonically; "below"
+// holds on one end of the row and "above" on the other, so each bit flips at most once.
+template <class P>
+__device__ __forceinline__ uint32_t fail_bits(const SurfTri& S, const RowK& K, float ux, int x) {
+	const float px = __fmul_rn(__int2float_rn(x), ux);
+	float s;
+	if constexpr (P::plane == 1) s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.nx, px, K.kpl));
+	else if constexpr (P::plane == 2) s = __fadd_rn(__fmaf_rn(S.nx, px, K.kpl), K.kpl2);
+	else s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.ny, K.py, __fmul_rn(S.nx, px)));
+	const float a = __fadd_rn(s, S.d1), b = __fadd_rn(s, S.d2);
+	const bool pf = __fmul_rn(a, b) > 0.0f;
+	uint32_t f = (pf && a < 0.0f ? 1u : 0u) | (pf && a > 0.0f ? 2u : 0u);
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		float v;
+		if constexpr (P::edge_xy == 1) v = __fmaf_rn(S.exy[i][0], px, K.kxy[i]);
+		else v = __fmaf_rn(S.exy[i][1], K.py, __fmul_rn(S.exy[i][0], px));
+		f |= (__fadd_rn(v, S.dxy[i]) < 0.0f ? 1u : 0u) << (2 + i);
+	}
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		float v;
+		if constexpr (P::edge_zx == 1) v = __fmaf_rn(S.ezx[i][0], K.pz, __fmul_rn(S.ezx[i][1], px));
+		else v = __fmaf_rn(S.ezx[i][1], px, K.kzx[i]);
+		f |= (__fadd_rn(v, S.dzx[i]) < 0.0f ? 1u : 0u) << (5 + i);
+	}
+	return f;
+}
+
+// YZ edge tests for row (y, z): independent of x.  Bit i set = YZ edge i fails.
+template <class P>
+__device__ __forceinline__ uint32_t yz_fail_bits(const SurfTri& S, float py, float pz) {
+	uint32_t f = 0;
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		const float v = mul_add<P::edge_yz>(S.eyz[i][0], py, S.eyz[i][1], pz);
+		f |= (__fadd_rn(v, S.dyz[i]) < 0.0f ? 1u : 0u) << i;
+	}
+	return f;
+}
+
+// Direction of every x-dependent test for this triangle: lo = passes on a suffix of x (a lower
+// bound), hi = passes on a prefix (an upper bound); tests in neither mask do not depend on x.
+struct RowDirs {
+	uint32_t lo, hi;
+	float inv[8];    // -1 / (coefficient of x in the test, in voxels): x* = (row term + d) * inv
+};
+
+__device__ __forceinline__ void row_dirs(const SurfTri& S, float ux, RowDirs& D) {
+	D.lo = 0; D.hi = 0;
+	// plane: s increases with x when n.x > 0. "below" (bit 0) then holds on a prefix -> lower bound.
+	if (S.nx > 0.0f) { D.lo |= 1u; D.hi |= 2u; }
+	else if (S.nx < 0.0f) { D.lo |= 2u; D.hi |= 1u; }
+	const float ipl = -1.0f / (S.nx * ux);
+	D.inv[0] = ipl; D.inv[1] = ipl;
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		const float cxy = S.exy[i][0], czx = S.ezx[i][1];
+		if (cxy > 0.0f) D.lo |= 1u << (2 + i); else if (cxy < 0.0f) D.hi |= 1u << (2 + i);
+		if (czx > 0.0f) D.lo |= 1u << (5 + i); else if (czx < 0.0f) D.hi |= 1u << (5 + i);
+		D.inv[2 + i] = -1.0f / (cxy * ux);
+		D.inv[5 + i] = -1.0f / (czx * ux);
+	}
+}
+
+// Real-valued crossing of test i (in voxel x units) for the row.
+__device__ __forceinline__ float crossing(const SurfTri& S, const RowDirs& D, float py, float pz, int i) {
+	if (i == 0) return (S.ny * py + S.nz * pz + S.d1) * D.inv[0];
+	if (i == 1) return (S.ny * py + S.nz * pz + S.d2) * D.inv[1];
+	if (i < 5) return (S.exy[i - 2][1] * py + S.dxy[i - 2]) * D.inv[i];
+	return (S.ezx[i - 5][0] * pz + S.dzx[i - 5]) * D.inv[i];
+}
+
+// Exact pass interval of row (y, z) within [bx0, bx1].  Returns false if the row is empty.
+// Correct for any estimate quality: the estimates only choose where the exact walk starts.
+template <class P>
+__device__ __forceinline__ bool row_interval(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int& xl,
+                                             int& xh) {
+	const int bx0 = S.bx0, bx1 = S.bx1;
+	const uint32_t cmask = ~(D.lo | D.hi) & 0xFFu;
+	// tests that do not depend on x: evaluate once
+	if (cmask && (fail_bits<P>(S, K, ux, bx0) & cmask)) return false;
+	// candidate ends from the real-valued crossings
+	float elo = (float)bx0, ehi = (float)bx1;
+#pragma unroll
+	for (int i = 0; i < 8; i++) {
+		const uint32_t bit = 1u << i;
+		if ((D.lo | D.hi) & bit) {
+			const float c = crossing(S, D, K.py, K.pz, i);
+			if (D.lo & bit) elo = fmaxf(elo, ceilf(c));
+			else ehi = fminf(ehi, floorf(c));
+		}
+	}
+	// lower end: first x with every lower-bound test passing
+	int e = (int)fminf(fmaxf(elo, (float)bx0), (float)bx1);
+	if (!(fail_bits<P>(S, K, ux, e) & D.lo)) {
+		while (e > bx0 && !(fail_bits<P>(S, K, ux, e - 1) & D.lo)) e--;
+	} else {
+		do { e++; } while (e <= bx1 && (fail_bits<P>(S, K, ux, e) & D.lo));
+		if (e > bx1) return false;
+	}
+	xl = e;
+	// upper end: last x >= xl with every upper-bound test passing
+	int f = (int)fminf(fmaxf(ehi, (float)xl), (float)bx1);
+	if (!(fail_bits<P>(S, K, ux, f) & D.hi)) {
+		while (f < bx1 && !(fail_bits<P>(S, K, ux, f + 1) & D.hi)) f++;
+	} else {
+		do { f--; } while (f >= xl && (fail_bits<P>(S, K, ux, f) & D.hi));
+		if (f < xl) return false;
+	}
+	xh = f;
+	return true;
+}
+
+// Pass interval of the YZ tests along y for a fixed z slice, within [by0, by1] (same scheme:
+// every YZ test is monotone in p.y).
+template <class P>
+__device__ __forceinline__ bool y_interval(const SurfTri& S, float uy, float pz, int& ya, int& yb) {
+	uint32_t lo = 0, hi = 0;
+	float elo = (float)S.by0, ehi = (float)S.by1;
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		const float a = S.eyz[i][0];
+		if (a > 0.0f) lo |= 1u << i; else if (a < 0.0f) hi |= 1u << i;
+		if (a != 0.0f) {
+			const float c = -(S.eyz[i][1] * pz + S.dyz[i]) / (a * uy);
+			if (a > 0.0f) elo = fmaxf(elo, ceilf(c)); else ehi = fminf(ehi, floorf(c));
+		}
+	}
+	const uint32_t cmask = ~(lo | hi) & 7u;
+	auto fails = [&](int y) { return yz_fail_bits<P>(S, __fmul_rn(__int2float_rn(y), uy), pz); };
+	if (cmask && (fails(S.by0) & cmask)) return false;
+	int e = (int)fminf(fmaxf(elo, (float)S.by0), (float)S.by1);
+	if (!(fails(e) & lo)) {
+		while (e > S.by0 && !(fails(e - 1) & lo)) e--;
+	} else {
+		do { e++; } while (e <= S.by1 && (fails(e) & lo));
+		if (e > S.by1) return false;
+	}
+	ya = e;
+	int f = (int)fminf(fmaxf(ehi, (float)ya), (float)S.by1);
+	if (!(fails(f) & hi)) {
+		while (f < S.by1 && !(fails(f + 1) & hi)) f++;
+	} else {
+		do { f--; } while (f >= ya && (fails(f) & hi));
+		if (f < ya) return false;
+	}
+	yb = f;
+	return true;
+}
+
+// Write the bits of row (y, z), x in [xl, xh].  Linear index x + y*gx + z*gx*gy (:175-178).
+__device__ __forceinline__ void write_row(uint32_t* table, bool morton, const uint32_t* grid, int y, int z, int xl,
+                                          int xh) {
+	if (morton) {
+		or_span_morton(table, xl, xh, (uint32_t)y, (uint32_t)z);
+	} else {
+		const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
+		or_span(table, base + (uint64_t)xl, base + (uint64_t)xh);
+	}
+}
+
+}  // namespace cvx

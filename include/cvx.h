@@ -1,0 +1,138 @@
+/*
+ * cvx.h -- C ABI of the GB300 voxelization engine (cuda_voxelizer_gb300).
+ *
+ * Drop-in for the voxelization path of Forceflow/cuda_voxelizer v0.6: surface voxelization
+ * (`voxelize`, src/voxelize.cu:192-238) and solid voxelization (`voxelize_solid`,
+ * src/voxelize_solid.cu:147-193) of an fp32 triangle soup into a bit-packed uint32 table, in linear
+ * or Morton order.  Plain pointers and sizes only; device pointers may be cudaMalloc'ed or managed
+ * memory (the reference's callers pass cudaMallocManaged buffers, src/main.cpp:66,214).
+ *
+ * Semantics kept from the reference:
+ *   - the table holds ceil(gx*gy*gz/32) words; voxel (x,y,z) is linear index x + y*gx + z*gx*gy
+ *     (src/voxelize.cu:175-178) or its Morton code (src/voxelize.cuh:20-34); word = idx/32 and the
+ *     bit is 31 - idx%32, most significant bit first (src/voxelize.cu:50-55, src/util.h:25-38);
+ *   - surface ORs into the table and solid XORs into it, so the caller zeroes it first
+ *     (the reference relies on fresh managed pages, src/main.cpp:214);
+ *   - every bit is identical to the reference kernels' result on the same input.
+ * Differences, all at the interface: calls are asynchronous on the given stream, return a status
+ * instead of calling exit(), never print, and allocate their scratch once per (device, stream)
+ * (see cvx_voxelize_ws for caller-owned scratch).  The C++ symbols with the reference's exact
+ * signatures are declared in cvx_dropin.h.
+ */
+#ifndef CVX_H_
+#define CVX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CVX_VERSION_MAJOR 1
+#define CVX_VERSION_MINOR 0
+
+/* Same bytes as the reference's voxinfo (src/util.h:50-69) on LP64 targets:
+ * AABox<float3> bbox @0, uint3 gridsize @24, size_t n_triangles @40, float3 unit @48, 64 bytes. */
+typedef struct cvx_voxinfo {
+	float bbox_min[3];
+	float bbox_max[3];
+	uint32_t gridsize[3];
+	uint32_t _pad0;
+	uint64_t n_triangles;
+	float unit[3];
+	uint32_t _pad1;
+} cvx_voxinfo;
+
+typedef enum cvx_status {
+	CVX_OK = 0,
+	CVX_ERR_INVALID_VALUE = 1,   /* null pointer, zero grid, bad size */
+	CVX_ERR_UNSUPPORTED = 2,     /* e.g. Morton order on a grid that is not a cubic power of two */
+	CVX_ERR_OUT_OF_MEMORY = 3,   /* scratch allocation failed */
+	CVX_ERR_CUDA = 4,            /* a CUDA runtime call failed (see cvx_last_error_message) */
+	CVX_ERR_DEVICE_CHECK = 5,    /* a device-side check reported a problem (cvx_device_status) */
+	CVX_ERR_CAPTURING = 6        /* the call would allocate while the stream is being captured */
+} cvx_status;
+
+/* cudaStream_t without including the CUDA headers (the same type). */
+typedef struct CUstream_st* cvx_stream_t;
+
+const char* cvx_status_string(cvx_status s);
+/* Message of the last failed call on this host thread. */
+const char* cvx_last_error_message(void);
+int cvx_version(void); /* MAJOR*1000 + MINOR */
+
+/* ---- host-side setup (replaces src/util.h:56-61, :80-110 and src/main.cpp:179,190) ---------- */
+
+/* voxinfo constructor: unit = (bbox_max - bbox_min) / float(gridsize), per axis. */
+cvx_status cvx_voxinfo_init(cvx_voxinfo* out, const float bbox_min[3], const float bbox_max[3],
+                            const uint32_t gridsize[3], uint64_t n_triangles);
+/* createMeshBBCube: pad the box to a cube, then by extent/10001 on every side. */
+cvx_status cvx_bbox_cube(const float in_min[3], const float in_max[3], float out_min[3], float out_max[3]);
+/* Vertex min/max of a host triangle soup (9 floats per triangle); what Trimesh need_bbox computes. */
+cvx_status cvx_mesh_bbox(const float* triangles, uint64_t n_triangles, float out_min[3], float out_max[3]);
+/* Words of the bit table: ceil(gx*gy*gz / 32), computed exactly (src/main.cpp:190 goes through a
+ * float ceil, which is exact for power-of-two grids). */
+uint64_t cvx_table_words(const cvx_voxinfo* info);
+
+/* ---- single mesh ------------------------------------------------------------------------------ */
+
+/* Surface voxelization; replaces voxelize() (src/voxelize.cu:192) and its kernel voxelize_triangle
+ * (src/voxelize.cu:58).  ORs into d_table.  morton != 0 needs a cubic power-of-two grid. */
+cvx_status cvx_voxelize(const cvx_voxinfo* info, const float* d_triangles, uint32_t* d_table, int morton,
+                        cvx_stream_t stream);
+
+/* Solid voxelization; replaces voxelize_solid() (src/voxelize_solid.cu:147) and its kernel
+ * voxelize_triangle_solid (src/voxelize_solid.cu:73).  XORs into d_table. */
+cvx_status cvx_voxelize_solid(const cvx_voxinfo* info, const float* d_triangles, uint32_t* d_table, int morton,
+                              cvx_stream_t stream);
+
+/* Bytes of caller-owned scratch needed by cvx_voxelize_ws for this mesh and mode. */
+uint64_t cvx_workspace_size(const cvx_voxinfo* info, int solid);
+
+/* cvx_voxelize / cvx_voxelize_solid with caller-owned scratch (no allocation inside; usable while
+ * the stream is being captured into a CUDA graph).  d_workspace: device memory of at least
+ * cvx_workspace_size() bytes, 256-byte aligned; its contents need not be preserved between calls. */
+cvx_status cvx_voxelize_ws(const cvx_voxinfo* info, const float* d_triangles, uint32_t* d_table, int morton,
+                           int solid, void* d_workspace, uint64_t workspace_bytes, cvx_stream_t stream);
+
+/* Synchronizes `stream` and reports device-side checks of the last calls made on it through the
+ * library-owned scratch: CVX_OK, or CVX_ERR_DEVICE_CHECK (a queue overflow or a timed-out copy). */
+cvx_status cvx_device_status(cvx_stream_t stream);
+
+/* ---- batches: many meshes of different sizes, grids and modes in one launch sequence ---------- */
+
+typedef struct cvx_job {
+	cvx_voxinfo info;
+	const float* d_triangles;
+	uint32_t* d_table;
+	int32_t morton;
+	int32_t solid;
+} cvx_job;
+
+/* All jobs in one launch sequence (a fixed handful of kernels whatever the job count); the
+ * tables of different jobs must not overlap.  Results are bit-identical to one call per job. */
+cvx_status cvx_voxelize_batch(const cvx_job* jobs, uint32_t n_jobs, cvx_stream_t stream);
+
+/* A batch prepared once and replayed as one CUDA graph launch. */
+typedef struct cvx_plan cvx_plan;
+#define CVX_PLAN_CLEAR_TABLES 1u /* the graph zeroes every job's table before voxelizing */
+cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out);
+cvx_status cvx_plan_launch(cvx_plan* plan, cvx_stream_t stream);
+cvx_status cvx_plan_destroy(cvx_plan* plan);
+
+/* ---- tuning ---------------------------------------------------------------------------------- */
+
+typedef struct cvx_tuning {
+	uint32_t small_vox;   /* surface: triangles with at most this many bbox voxels stay in one thread */
+	uint32_t small_cols;  /* solid: triangles with at most this many columns stay in one thread */
+} cvx_tuning;
+/* Per-device tuning used by subsequent calls (results never depend on it). */
+cvx_status cvx_get_tuning(int device, cvx_tuning* out);
+cvx_status cvx_set_tuning(int device, const cvx_tuning* in);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* CVX_H_ */

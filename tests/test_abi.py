@@ -1,0 +1,102 @@
+"""CPU tests of the C ABI: the library loads, exports every function declared in include/*.h, the
+voxinfo layout is the reference's, and argument validation answers without touching a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from cuda_voxelizer_gb300 import _lib
+from cuda_voxelizer_gb300 import api as cv
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in ("cvx.h",):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(cvx_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "cvx_voxelize" in names and "cvx_voxelize_solid" in names and len(names) >= 15
+
+
+@pytest.mark.parametrize("name", declared_functions())
+def test_every_declared_function_is_exported(name):
+    assert hasattr(_lib.lib, name)
+    assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_dropin_cxx_symbols_exported():
+    # void voxelize(const voxinfo&, float*, unsigned int*, bool) and voxelize_solid(...), C++ linkage
+    for sym in ("_Z8voxelizeRK7voxinfoPfPjb", "_Z14voxelize_solidRK7voxinfoPfPjb"):
+        assert hasattr(_lib.lib, sym)
+
+
+def test_voxinfo_layout_matches_reference():
+    V = _lib.CvxVoxinfo
+    assert ctypes.sizeof(V) == 64
+    assert V.bbox_min.offset == 0 and V.bbox_max.offset == 12
+    assert V.gridsize.offset == 24 and V.n_triangles.offset == 40 and V.unit.offset == 48
+
+
+def test_version_and_status_strings():
+    assert _lib.lib.cvx_version() >= 1000
+    assert _lib.lib.cvx_status_string(0) == b"CVX_OK"
+    assert _lib.lib.cvx_status_string(2) == b"CVX_ERR_UNSUPPORTED"
+
+
+def _info(g=64, n=1):
+    return cv.make_info((0, 0, 0), (1, 1, 1), g, n)
+
+
+def test_validation_rejects_null_and_zero_grid():
+    info = _info()
+    assert _lib.lib.cvx_voxelize(None, 1, 1, 0, None) == 1
+    assert _lib.lib.cvx_voxelize(ctypes.byref(info), None, 1, 0, None) == 1
+    assert _lib.lib.cvx_voxelize(ctypes.byref(info), 1, None, 0, None) == 1
+    bad = _info()
+    bad.gridsize[1] = 0
+    assert _lib.lib.cvx_voxelize_solid(ctypes.byref(bad), 1, 1, 0, None) == 1
+    assert b"gridsize" in _lib.lib.cvx_last_error_message()
+
+
+def test_morton_needs_cubic_power_of_two():
+    for g in ((100, 100, 100), (64, 64, 32)):
+        info = cv.make_info((0, 0, 0), (1, 1, 1), g, 1)
+        assert _lib.lib.cvx_voxelize(ctypes.byref(info), 1, 1, 1, None) == 2
+        assert _lib.lib.cvx_voxelize_solid(ctypes.byref(info), 1, 1, 1, None) == 2
+
+
+def test_empty_mesh_is_a_no_op():
+    info = _info(n=0)
+    assert _lib.lib.cvx_voxelize(ctypes.byref(info), None, 1, 0, None) == 0
+
+
+def test_workspace_size():
+    info = _info(64, 1000)
+    s = _lib.lib.cvx_workspace_size(ctypes.byref(info), 0)
+    d = _lib.lib.cvx_workspace_size(ctypes.byref(info), 1)
+    assert s >= 1000 * 32 and d >= s + 64 ** 3 // 8
+
+
+def test_ws_rejects_small_or_misaligned_workspace():
+    info = _info(64, 10)
+    need = _lib.lib.cvx_workspace_size(ctypes.byref(info), 0)
+    assert _lib.lib.cvx_voxelize_ws(ctypes.byref(info), 1, 1, 0, 0, 256, need - 1, None) == 1
+    assert _lib.lib.cvx_voxelize_ws(ctypes.byref(info), 1, 1, 0, 0, 257, need, None) == 1
+
+
+def test_mesh_bbox_host():
+    t = np.array([[0, 1, 2, 3, -4, 5, 6, 7, 8]], dtype=np.float32)
+    lo, hi = cv.mesh_bbox(t)
+    assert list(lo) == [0, -4, 2] and list(hi) == [6, 7, 8]
+    with pytest.raises(cv.CvxError):
+        cv.mesh_bbox(np.zeros((0, 9), np.float32))

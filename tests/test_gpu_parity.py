@@ -1,0 +1,286 @@
+"""GPU parity: the engine against the reference's own CUDA kernels and its CPU voxelizer.
+
+* Bit-exact against the reference kernels voxelize_triangle / voxelize_triangle_solid
+  (src/voxelize.cu:58, src/voxelize_solid.cu:73), compiled from the reference sources for sm_103a
+  (oracle/build_ref.sh) and run by oracle/ref_gpu_runner.cu on the same device buffers: the
+  golden meshes, the 64^3 torus, the 512^3 displaced icosphere (surface and solid, linear and
+  Morton), triangle-size-stress soups at 1024^3, and edge cases (degenerate, grid-aligned,
+  axis-aligned and out-of-bbox triangles, tiny / odd / non-cubic grids, empty meshes).
+* Against the reference CPU voxelizer (the golden fixtures): every differing bit is counted and
+  traced to a boundary tie (tests/tie_trace.py).  Tolerance: a difference is a tie when a predicate
+  is within 1e-4 voxel (surface) / 1e-3 (solid column decision) of its boundary in float64.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import oracle  # noqa: E402
+from cuda_voxelizer_gb300 import api as cv  # noqa: E402
+from cuda_voxelizer_gb300 import meshgen  # noqa: E402
+from golden_data import arrays, manifest, mesh, table_keys  # noqa: E402
+import tie_trace  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+MODES = [(False, False), (True, False), (False, True), (True, True)]
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return oracle.RefGPU()
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+GUARD = 256  # zero words after every table: a write past the end shows up as a difference
+
+
+def run_engine(info, t_dev, morton, solid):
+    table = torch.zeros(cv.table_words(info) + GUARD, dtype=torch.int32, device="cuda")
+    (cv.voxelize_solid if solid else cv.voxelize)(info, t_dev, table, morton)
+    return table
+
+
+def run_ref(ref, info, t_dev, morton, solid):
+    table = torch.zeros(cv.table_words(info) + GUARD, dtype=torch.int32, device="cuda")
+    ref.voxelize(bytes(info), t_dev.data_ptr(), table.data_ptr(), morton, solid, _stream())
+    return table
+
+
+def compare(ref, tris, info, morton, solid):
+    t = torch.from_numpy(np.ascontiguousarray(tris, dtype=np.float32).reshape(-1)).cuda()
+    a = run_engine(info, t, morton, solid)
+    b = run_ref(ref, info, t, morton, solid)
+    torch.cuda.synchronize()
+    cv.device_status()
+    a = a.cpu().numpy().view(np.uint32)
+    b = b.cpu().numpy().view(np.uint32)
+    return a, b
+
+
+def assert_same(a, b, what):
+    d = np.nonzero(a != b)[0]
+    pa = int(np.unpackbits(a.view(np.uint8)).sum())
+    pb = int(np.unpackbits(b.view(np.uint8)).sum())
+    assert d.size == 0, f"{what}: {d.size} words differ (engine {pa} bits, reference {pb} bits), first {d[:8]}"
+
+
+def info_of(tris, g):
+    return cv.make_voxinfo(tris, g)
+
+
+# ---- bit-exact against the reference kernels ----------------------------------------------------
+
+@pytest.mark.parametrize("name,key,morton,solid", table_keys())
+def test_golden_meshes_vs_reference_kernels(ref, name, key, morton, solid):
+    c = manifest()["cases"][name]
+    info = cv.VoxInfo.from_buffer_copy(bytes.fromhex(c["voxinfo_hex"]))
+    a, b = compare(ref, mesh(name), info, morton, solid)
+    assert_same(a, b, key)
+
+
+@pytest.mark.parametrize("morton,solid", MODES)
+def test_torus_64(ref, morton, solid):
+    t = meshgen.torus(0)
+    a, b = compare(ref, t, info_of(t, 64), morton, solid)
+    assert_same(a, b, "torus64")
+
+
+@pytest.fixture(scope="module")
+def ico8():
+    return meshgen.icosphere(0, level=8)
+
+
+@pytest.mark.parametrize("morton,solid", MODES)
+def test_icosphere_512(ref, ico8, morton, solid):
+    a, b = compare(ref, ico8, info_of(ico8, 512), morton, solid)
+    assert_same(a, b, "ico8@512")
+
+
+@pytest.mark.parametrize("seed,n", [(1, 20_000), (2, 200_000)])
+def test_soup_1024(ref, seed, n):
+    t = meshgen.soup(seed, n=n)
+    a, b = compare(ref, t, info_of(t, 1024), False, False)
+    assert_same(a, b, f"soup{n}@1024")
+
+
+@pytest.mark.parametrize("solid", [False, True])
+def test_soup_dense_512_solid_and_surface(ref, solid):
+    t = meshgen.soup(3, n=30_000, lmin=0.5 / 512, lmax=0.2)
+    a, b = compare(ref, t, info_of(t, 512), False, solid)
+    assert_same(a, b, "soup30k@512")
+
+
+def _adversarial(seed, g):
+    rng = np.random.default_rng(seed)
+    parts = []
+    s = meshgen.soup(seed, n=3000, lmin=0.3 / g, lmax=0.4)
+    parts.append(s)
+    q = s[:500].copy()
+    q = np.round(q * g * 2) / (g * 2)                  # vertices on voxel faces and centres
+    parts.append(q)
+    a = s[500:900].copy().reshape(-1, 3, 3)
+    a[:, :, rng.integers(0, 3)] = a[:, :1, rng.integers(0, 3)]  # axis-aligned planes
+    parts.append(a.reshape(-1, 9))
+    d = s[900:1000].copy().reshape(-1, 3, 3)
+    d[:50, 1] = d[:50, 0]                               # zero-area: repeated vertex
+    d[50:, 2] = 0.5 * (d[50:, 0] + d[50:, 1])           # collinear
+    parts.append(d.reshape(-1, 9))
+    return np.concatenate(parts).astype(np.float32)
+
+
+@pytest.mark.parametrize("g", [8, 37, 64, 100, 256])
+@pytest.mark.parametrize("morton,solid", MODES)
+def test_adversarial_vs_reference_kernels(ref, g, morton, solid):
+    if morton and g & (g - 1):
+        pytest.skip("Morton order needs a power-of-two grid")
+    t = _adversarial(g, g)
+    a, b = compare(ref, t, info_of(t, g), morton, solid)
+    assert_same(a, b, f"adversarial g={g}")
+
+
+@pytest.mark.parametrize("solid", [False, True])
+def test_non_cubic_grid(ref, solid):
+    t = meshgen.icosphere(4, level=4)
+    info = cv.make_voxinfo(t, 64)
+    info.gridsize[0], info.gridsize[1], info.gridsize[2] = 96, 64, 40
+    for i, gdim in enumerate((96, 64, 40)):
+        info.unit[i] = np.float32((np.float32(info.bbox_max[i]) - np.float32(info.bbox_min[i])) / np.float32(gdim))
+    a, b = compare(ref, t, info, False, solid)
+    assert_same(a, b, "non-cubic")
+
+
+@pytest.mark.parametrize("solid", [False, True])
+def test_triangles_outside_bbox(ref, solid):
+    """The caller's bbox covers only part of the mesh: surface clamps to the grid; solid columns
+    whose row range runs past x = gx continue into the next rows, exactly as in the reference."""
+    t = meshgen.icosphere(5, level=4)
+    info = cv.make_voxinfo(t, 64)
+    for i in range(3):  # shrink the box towards its low corner: many vertices beyond bbox_max
+        info.bbox_max[i] = np.float32(info.bbox_min[i] + 0.7 * (info.bbox_max[i] - info.bbox_min[i]))
+        info.unit[i] = np.float32((np.float32(info.bbox_max[i]) - np.float32(info.bbox_min[i])) / np.float32(64))
+    # Solid: keep triangles whose columns lie in rows y, z <= 0.9 g, so that a row range running past
+    # x = gx continues into a following row inside the table (past the table's end, and for columns
+    # outside the grid, the reference writes out of bounds).
+    lim = np.array(info.bbox_min[1:], np.float32) + 0.9 * (np.array(info.bbox_max[1:], np.float32) -
+                                                            np.array(info.bbox_min[1:], np.float32))
+    keep = np.all(t.reshape(-1, 3, 3)[:, :, 1:] >= np.array(info.bbox_min[1:], np.float32), axis=(1, 2))
+    keep &= np.all(t.reshape(-1, 3, 3)[:, :, 1:] <= lim, axis=(1, 2))
+    t = np.ascontiguousarray(t[keep]) if solid else t
+    info.n_triangles = t.shape[0]
+    a, b = compare(ref, t, info, False, solid)
+    assert_same(a, b, "outside-bbox")
+
+
+def test_empty_mesh():
+    info = cv.make_info((0, 0, 0), (1, 1, 1), 32, 0)
+    table = torch.zeros(cv.table_words(info) + GUARD, dtype=torch.int32, device="cuda")
+    cv.voxelize(info, torch.zeros(9, device="cuda"), table)
+    cv.voxelize_solid(info, torch.zeros(9, device="cuda"), table)
+    torch.cuda.synchronize()
+    assert int(table.abs().sum()) == 0
+
+
+def test_accumulates_into_existing_table(ref):
+    """Surface ORs into the caller's table and solid XORs into it, like the reference."""
+    t = meshgen.torus(3)
+    info = info_of(t, 64)
+    td = torch.from_numpy(t.reshape(-1)).cuda()
+    init = torch.randint(-2 ** 31, 2 ** 31 - 1, (cv.table_words(info) + GUARD,), dtype=torch.int32, device="cuda")
+    for solid in (False, True):
+        a = init.clone()
+        b = init.clone()
+        (cv.voxelize_solid if solid else cv.voxelize)(info, td, a, False)
+        ref.voxelize(bytes(info), td.data_ptr(), b.data_ptr(), False, solid, _stream())
+        torch.cuda.synchronize()
+        assert torch.equal(a, b)
+
+
+# ---- against the reference CPU voxelizer: differences are ties --------------------------------
+
+@pytest.mark.parametrize("name,key,morton,solid", [k for k in table_keys() if not k[2]])
+def test_cpu_differences_are_ties(name, key, morton, solid):
+    c = manifest()["cases"][name]
+    info = cv.VoxInfo.from_buffer_copy(bytes.fromhex(c["voxinfo_hex"]))
+    tris = mesh(name)
+    got = cv.voxelize_host(info, tris, morton=False, solid=solid)
+    want = arrays()[key]
+    bits = tie_trace.diff_bits(got, want)
+    if bits.size == 0:
+        return
+    grid = np.frombuffer(bytes(info), np.uint32, 3, 24)
+    x, y, z = tie_trace.linear_to_xyz(bits, grid, False)
+    if not solid:
+        m = tie_trace.surface_margin(tris, bytes(info), np.stack([x, y, z], 1))
+        assert np.all(m < 1e-4), f"{key}: {bits.size} differing bits, untraced margins {np.sort(m)[-5:]}"
+    else:
+        rows = sorted(set(zip(y.tolist(), z.tolist())))
+        m = tie_trace.solid_row_margin(tris, bytes(info), rows)
+        assert np.all(m < 1e-3), f"{key}: {bits.size} differing bits in {len(rows)} rows, untraced {np.sort(m)[-5:]}"
+
+
+# ---- batch, plan and caller-owned scratch give the same bits --------------------------------------
+
+def _mixed_jobs():
+    specs = [(meshgen.torus(10), 64, False, False), (meshgen.icosphere(11, 5), 128, True, False),
+             (meshgen.icosphere(12, 4), 64, False, True), (meshgen.torus(13, nu=40, nv=20), 128, True, True),
+             (meshgen.soup(14, n=5000, lmin=0.01, lmax=0.3), 256, False, False),
+             (meshgen.icosphere(15, 6), 100, False, True)]
+    jobs = []
+    for t, g, morton, solid in specs:
+        info = info_of(t, g)
+        td = torch.from_numpy(t.reshape(-1)).cuda()
+        jobs.append(cv.Job(info, td, torch.zeros(cv.table_words(info) + GUARD, dtype=torch.int32, device="cuda"),
+                           morton, solid))
+    return jobs
+
+
+def test_batch_equals_single_calls():
+    jobs = _mixed_jobs()
+    cv.voxelize_batch(jobs)
+    torch.cuda.synchronize()
+    cv.device_status()
+    for j in jobs:
+        single = run_engine(j.info, j.triangles, j.morton, j.solid)
+        torch.cuda.synchronize()
+        assert torch.equal(single, j.table)
+
+
+def test_plan_equals_single_calls_and_replays():
+    jobs = _mixed_jobs()
+    plan = cv.Plan(jobs, clear_tables=True)
+    for _ in range(3):
+        plan.launch()
+    torch.cuda.synchronize()
+    for j in jobs:
+        single = run_engine(j.info, j.triangles, j.morton, j.solid)
+        torch.cuda.synchronize()
+        assert torch.equal(single, j.table)
+    plan.close()
+
+
+@pytest.mark.parametrize("solid", [False, True])
+def test_caller_workspace_equals_internal(solid):
+    t = meshgen.soup(20, n=20000, lmin=0.002, lmax=0.3)
+    info = info_of(t, 256)
+    td = torch.from_numpy(t.reshape(-1)).cuda()
+    ws = torch.empty(cv.workspace_size(info, solid), dtype=torch.uint8, device="cuda")
+    a = torch.zeros(cv.table_words(info) + GUARD, dtype=torch.int32, device="cuda")
+    cv.voxelize_ws(info, td, a, ws, morton=False, solid=solid)
+    b = run_engine(info, td, False, solid)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+
+
+def test_repeated_calls_are_identical():
+    t = meshgen.icosphere(21, 6)
+    info = info_of(t, 256)
+    td = torch.from_numpy(t.reshape(-1)).cuda()
+    for morton in (False, True):
+        for solid in (False, True):
+            outs = [run_engine(info, td, morton, solid) for _ in range(3)]
+            torch.cuda.synchronize()
+            assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
