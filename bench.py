@@ -1,0 +1,407 @@
+"""Benchmark of the voxelization hot path (one JSON line on stdout).
+
+Workload (one "step"): the displaced icosphere subdivided 8 times (1,310,720 fp32 triangles, seeded
+synthetic mesh) voxelized at 512^3 four times -- surface and solid, linear and Morton order -- each
+into a freshly zeroed bit table.  Metric: Mtris/s (triangles voxelized per second, 4 x 1.31M per
+step).  Inputs (47 MB of triangles, 4 x 16 MiB of tables) are smaller than the 129 MB L2, so L2 is
+flushed (a 512 MiB write) between timed steps, outside the timed region.
+
+Keys beyond the base contract:
+  e2e          the same metric through the public host-buffer path: pinned host triangles copied in,
+               four voxelizations, four tables copied out, all inside the timed region.
+  roofline     the step's dominant kernel against the measured HBM copy bandwidth
+               (MEASURED_PEAKS.json), with DRAM traffic from the committed ncu summary when present.
+  cpu_baseline the reference CPU algorithm (oracle port, OpenMP with a critical section per bit, as
+               src/cpu_voxelizer.cpp runs) on a contiguous 1/32 sample of the same triangles.
+  extras       the triangle-size stress soup (2M triangles at 1024^3) against the reference CUDA kernel
+               rebuilt for sm_103a, and the 256-mesh batched workload against plain per-mesh calls.
+
+--impl reference times the reference's CPU implementation of the path (the oracle port on hosts
+where the reference's own x86 build cannot run) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+MODES = [(False, False), (True, False), (False, True), (True, True)]  # (morton, solid)
+METRIC = "Mtris/s voxelized (icosphere 1.31M tris, 512^3, surface+solid x linear+Morton)"
+SAMPLE_FRACTION = 32
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    p.add_argument("--no-extras", action="store_true", help="skip the soup / batch side measurements")
+    return p.parse_args()
+
+
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], [], set()
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+def cpu_sample(tris):
+    n = tris.shape[0] // SAMPLE_FRACTION
+    return np.ascontiguousarray(tris[:n])
+
+
+def time_cpu_reference(info_bytes, sample, threads):
+    """Reference CPU algorithm over the 4 modes on the sample; returns seconds."""
+    import oracle
+    t0 = time.perf_counter()
+    for morton, solid in MODES:
+        oracle.voxelize_omp(info_bytes, sample, morton=morton, solid=solid, threads=threads)
+    return time.perf_counter() - t0
+
+
+def run_reference_arm(args, rank, world):
+    """--impl reference: the reference's CPU implementation (OpenMP) on a bounded sample."""
+    if rank != 0:
+        return
+    import oracle
+    from cuda_voxelizer_gb300 import meshgen
+    import cuda_voxelizer_gb300 as cv
+    tris = meshgen.icosphere(0, level=8)
+    info = bytes(cv.make_voxinfo(tris, 512))
+    threads = os.cpu_count() or 1
+    sample = cpu_sample(tris)
+    kind = "reference" if oracle.ref_cpu_available() else "port"
+    for _ in range(args.warmup):
+        time_cpu_reference(info, sample[: max(1, sample.shape[0] // 8)], threads)
+    ts = [time_cpu_reference(info, sample, threads) for _ in range(args.steps)]
+    sec = float(np.mean(ts))
+    value = 4 * sample.shape[0] / sec / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere)",
+            "config": {"workload": "icosphere level 8 (1,310,720 tris) at 512^3, 4 modes; sample 1/32",
+                       "sample_triangles": int(sample.shape[0])},
+            "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": threads, "kind": kind,
+                             "sample": f"first {sample.shape[0]} of 1,310,720 triangles (1/{SAMPLE_FRACTION}), "
+                                       "4 modes, OpenMP parallel-for with a critical section per bit"},
+            "e2e": {"value": value, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+    import torch
+    import cuda_voxelizer_gb300 as cv
+    from cuda_voxelizer_gb300 import meshgen
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    tris = meshgen.icosphere(0, level=8)
+    info = cv.make_voxinfo(tris, 512)
+    T = tris.shape[0]
+    W = cv.table_words(info)
+    d_tris = torch.from_numpy(tris.reshape(-1)).cuda()
+    tables = [torch.empty(W, dtype=torch.int32, device="cuda") for _ in MODES]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        for (morton, solid), tab in zip(MODES, tables):
+            tab.zero_()
+            (cv.voxelize_solid if solid else cv.voxelize)(info, d_tris, tab, morton)
+
+    # ---- device-resident throughput -------------------------------------------------------------
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    launches_per_step = 2 + 2 + 3 + 5  # surface: classify+rows; solid: classify+cols+resolve (+morton+zero)
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+    barrier(world)
+    total_ms = max_over_ranks(float(sum(times)), world)
+    ms = total_ms / args.steps
+    value = world * 4 * T * args.steps / (total_ms / 1e3) / 1e6
+
+    # ---- per-kernel times for the roofline ------------------------------------------------------
+    cv.profile_enable(True)
+    prof = {}
+    reps = 5
+    for _ in range(reps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        step()
+        torch.cuda.synchronize()
+        for name, t in cv.profile_collect():
+            prof.setdefault(name, []).append(t)
+    cv.profile_enable(False)
+    kernel_ms = {k: float(np.sum(v)) / reps for k, v in prof.items()}
+    launches = {k: len(v) // reps for k, v in prof.items()}
+    dom = max(kernel_ms, key=kernel_ms.get)
+    # algorithmic bytes per launch: triangles read once (36 B each) + the table (g^3/8) for the
+    # classify kernels; flip table read + table write (2 g^3/8) for the solid resolve.
+    tbytes = 36 * T
+    table_bytes = W * 4
+    alg = {"surf_classify": tbytes + table_bytes, "solid_classify": tbytes, "surf_rows": 0, "solid_cols": 0,
+           "solid_resolve": 2 * table_bytes, "solid_morton": 2 * table_bytes, "solid_zero": table_bytes}
+    per_launch_ms = kernel_ms[dom] / max(1, launches[dom])
+    achieved = alg.get(dom, 0) / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = traffic_from_profiles(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "kernel_ms_per_step": kernel_ms, "alg_bytes_per_launch": alg.get(dom, 0)}
+
+    # ---- end to end through the public API with host buffers -------------------------------------
+    h_tris = torch.from_numpy(tris.reshape(-1)).pin_memory()
+    h_out = [torch.empty(W, dtype=torch.int32).pin_memory() for _ in MODES]
+
+    def e2e_step():
+        d_tris.copy_(h_tris, non_blocking=True)
+        step()
+        for tab, out in zip(tables, h_out):
+            out.copy_(tab, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e2e_step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        e2e_times.append(a.elapsed_time(b))
+    e2e_ms = max_over_ranks(float(np.mean(e2e_times)), world)
+    e2e = {"value": world * 4 * T / (e2e_ms / 1e3) / 1e6, "unit": "Mtris/s", "ms_per_step": e2e_ms,
+           "h2d_bytes_per_step": int(tris.nbytes), "d2h_bytes_per_step": int(4 * W * 4)}
+
+    # ---- parity spot check of what was timed (against the oracle's reference CPU algorithm) -------
+    extras = {}
+    line = {"metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced icosphere)",
+            "config": {"workload": "icosphere level 8 (1,310,720 tris) at 512^3; surface+solid x linear+Morton "
+                                   "per step", "gridsize": 512, "triangles": T, "l2": "flushed between steps "
+                                   "(512 MiB write, untimed)", "parallelism": f"replicas x{world}"},
+            "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps, "e2e": e2e,
+            "roofline": roofline}
+
+    if rank == 0:
+        import oracle
+        sample = cpu_sample(tris)
+        threads = os.cpu_count() or 1
+        sec = time_cpu_reference(bytes(info), sample, threads)
+        line["cpu_baseline"] = {"value": 4 * sample.shape[0] / sec / 1e6, "unit": "Mtris/s", "cores": threads,
+                                "kind": "reference" if oracle.ref_cpu_available() else "port",
+                                "sample": f"first {sample.shape[0]} of {T} triangles (1/{SAMPLE_FRACTION}), 4 modes, "
+                                          "OpenMP parallel-for with a critical section per bit"}
+        if not args.no_extras:
+            extras.update(bench_soup(cv, meshgen, torch, stream, flush))
+            extras.update(bench_batch(cv, meshgen, torch, stream))
+        line["extras"] = extras
+        print(json.dumps(line), flush=True)
+
+
+def bench_soup(cv, meshgen, torch, stream, flush):
+    """2M-triangle size-stress soup at 1024^3: engine vs the reference CUDA kernel (sm_103a build)."""
+    out = {}
+    tris = meshgen.soup(0, n=2_000_000)
+    info = cv.make_voxinfo(tris, 1024)
+    d = torch.from_numpy(tris.reshape(-1)).cuda()
+    tab = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+
+    def eng():
+        tab.zero_()
+        cv.voxelize(info, d, tab)
+
+    eng()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        eng()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    eng_ms = float(np.median(ts))
+    out["soup_1024"] = {"triangles": 2_000_000, "engine_ms": eng_ms, "engine_mtris_s": 2.0 / (eng_ms / 1e3)}
+    try:
+        import oracle
+        ref = oracle.RefGPU()
+        ref_tab = torch.zeros_like(tab)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ref.voxelize(bytes(info), d.data_ptr(), ref_tab.data_ptr(), False, False, stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        rms = a.elapsed_time(b)
+        out["soup_1024"].update({"ref_cuda_ms": rms, "speedup_vs_ref_cuda": rms / eng_ms,
+                                 "bit_exact_vs_ref_cuda": bool(torch.equal(tab, ref_tab))})
+    except Exception as e:  # reference cubins absent
+        out["soup_1024"]["ref_cuda"] = f"unavailable: {e}"
+    return out
+
+
+def bench_batch(cv, meshgen, torch, stream):
+    """256-mesh uneven mix: one graph launch (plan) vs plain per-mesh synchronous calls."""
+    specs = meshgen.batch_mix(0, 256)
+    jobs = []
+    for s in specs:
+        t = s.build()
+        info = cv.make_voxinfo(t, s.gridsize)
+        jobs.append(cv.Job(info, torch.from_numpy(t.reshape(-1)).cuda(),
+                           torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda"), s.morton, s.solid))
+    n_tris = sum(int(j.info.n_triangles) for j in jobs)
+    plan = cv.Plan(jobs, clear_tables=True)
+    for _ in range(3):
+        plan.launch()
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        plan.launch()
+    torch.cuda.synchronize()
+    plan_s = (time.perf_counter() - t0) / reps
+    # plain: what a caller of the reference drop-in does, one synchronous call per mesh
+    def plain():
+        for j in jobs:
+            j.table.zero_()
+            (cv.voxelize_solid if j.solid else cv.voxelize)(j.info, j.triangles, j.table, j.morton)
+            torch.cuda.synchronize()
+    plain()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        plain()
+    plain_s = (time.perf_counter() - t0) / reps
+    plan.close()
+    return {"batch_256": {"meshes": 256, "triangles": n_tris, "plan_ms": plan_s * 1e3, "plain_ms": plain_s * 1e3,
+                          "plan_meshes_s": 256 / plan_s, "plain_meshes_s": 256 / plain_s,
+                          "speedup_vs_plain": plain_s / plan_s}}
+
+
+if __name__ == "__main__":
+    main()

@@ -5,9 +5,9 @@ The native library ``_lib/libcvx.so`` is required; importing this package withou
 ImportError.
 """
 from .api import (CvxError, Job, Plan, VoxInfo, create_mesh_bbox_cube, device_status, get_tuning, make_info,
-                  make_voxinfo, mesh_bbox, set_tuning, table_words, voxelize, voxelize_batch, voxelize_host,
+                  make_voxinfo, mesh_bbox, profile_collect, profile_enable, set_tuning, table_words, voxelize, voxelize_batch, voxelize_host,
                   voxelize_solid, voxelize_ws, workspace_size)
 
 __all__ = ["CvxError", "Job", "Plan", "VoxInfo", "create_mesh_bbox_cube", "device_status", "get_tuning",
-           "make_info", "make_voxinfo", "mesh_bbox", "set_tuning", "table_words", "voxelize", "voxelize_batch",
+           "make_info", "make_voxinfo", "mesh_bbox", "profile_collect", "profile_enable", "set_tuning", "table_words", "voxelize", "voxelize_batch",
            "voxelize_host", "voxelize_solid", "voxelize_ws", "workspace_size"]

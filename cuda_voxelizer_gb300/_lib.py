@@ -59,6 +59,9 @@ SIGNATURES = {
     "cvx_plan_destroy": (c_status, [vp]),
     "cvx_get_tuning": (c_status, [ctypes.c_int, ctypes.POINTER(CvxTuning)]),
     "cvx_set_tuning": (c_status, [ctypes.c_int, ctypes.POINTER(CvxTuning)]),
+    "cvx_profile_enable": (c_status, [ctypes.c_int]),
+    "cvx_profile_collect": (ctypes.c_int, [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    "cvx_microbench_atomic_or": (ctypes.c_double, [vp, u64, ctypes.c_int, u32, u32]),
 }
 
 for _name, (_res, _args) in SIGNATURES.items():

@@ -19,7 +19,7 @@ from ._lib import CvxError, CvxJob, CvxTuning, CvxVoxinfo, check, lib
 
 __all__ = ["VoxInfo", "voxelize", "voxelize_solid", "voxelize_ws", "workspace_size", "create_mesh_bbox_cube",
            "mesh_bbox", "make_voxinfo", "table_words", "Job", "voxelize_batch", "Plan", "device_status",
-           "get_tuning", "set_tuning", "CvxError", "voxelize_host"]
+           "get_tuning", "set_tuning", "CvxError", "voxelize_host", "profile_enable", "profile_collect"]
 
 
 VoxInfo = CvxVoxinfo
@@ -187,6 +187,19 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def profile_enable(on: bool = True) -> None:
+    """Record per-kernel CUDA events for the calls of this thread (see profile_collect)."""
+    check(lib.cvx_profile_enable(int(bool(on))), "cvx_profile_enable")
+
+
+def profile_collect(max_entries: int = 4096) -> list:
+    """[(kernel name, ms), ...] of the calls made since the last collect, in launch order."""
+    names = (ctypes.c_char_p * max_entries)()
+    ms = (ctypes.c_float * max_entries)()
+    n = lib.cvx_profile_collect(names, ms, max_entries)
+    return [(names[i].decode(), float(ms[i])) for i in range(n)]
 
 
 def get_tuning(device: int = 0) -> dict:

@@ -82,6 +82,24 @@ cvx_status dev_state(DevState& out, int* dev_out = nullptr) {
 	return CVX_OK;
 }
 
+// ---- optional per-kernel timing (cvx_profile_*) --------------------------------------------------
+
+bool g_profile = false;
+struct Mark {
+	const char* name;
+	cudaEvent_t ev;
+};
+thread_local std::vector<Mark> t_marks;
+
+void prof_mark(void*, const char* name, cudaStream_t s) {
+	cudaEvent_t ev;
+	if (cudaEventCreate(&ev) != cudaSuccess) return;
+	cudaEventRecord(ev, s);
+	t_marks.push_back({name, ev});
+}
+const Prof g_prof{prof_mark, nullptr};
+const Prof* prof() { return g_profile ? &g_prof : nullptr; }
+
 // ---- scratch ------------------------------------------------------------------------------------
 
 struct RecLayout {
@@ -324,7 +342,7 @@ struct Runner {
 			cvx_status st = prepare(g, L);
 			if (st != CVX_OK) return st;
 			CVX_CUDA(cudaMemsetAsync(rec, 0, kCountersResetBytes, s));
-			CVX_CUDA(launch_surface(L, dev.tune, dev.rows_grid, s));
+			CVX_CUDA(launch_surface(L, dev.tune, dev.rows_grid, s, prof()));
 		}
 		if (!solid.empty()) {
 			for (Group& g : make_groups(solid, true)) {
@@ -332,13 +350,13 @@ struct Runner {
 				cvx_status st = prepare(g, L);
 				if (st != CVX_OK) return st;
 				CVX_CUDA(cudaMemsetAsync(rec, 0, kCountersResetBytes, s));
-				CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidToggles));
+				CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidToggles, prof()));
 			}
 			Group r = resolve_group(solid);
 			LaunchDesc L;
 			cvx_status st = prepare(r, L);
 			if (st != CVX_OK) return st;
-			CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidResolve));
+			CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidResolve, prof()));
 		}
 		return CVX_OK;
 	}
@@ -690,7 +708,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 			LaunchDesc L;
 			prep(g, L);
 			if (cudaMemsetAsync(p->rec, 0, kCountersResetBytes, cs) != cudaSuccess ||
-			    launch_surface(L, dev.tune, dev.rows_grid, cs) != cudaSuccess) {
+			    launch_surface(L, dev.tune, dev.rows_grid, cs, nullptr) != cudaSuccess) {
 				cst = cuda_fail(cudaGetLastError(), "capture surface");
 				break;
 			}
@@ -700,7 +718,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 				LaunchDesc L;
 				prep(g, L);
 				if (cudaMemsetAsync(p->rec, 0, kCountersResetBytes, cs) != cudaSuccess ||
-				    launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidToggles) != cudaSuccess) {
+				    launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidToggles, nullptr) != cudaSuccess) {
 					cst = cuda_fail(cudaGetLastError(), "capture solid");
 					break;
 				}
@@ -709,7 +727,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 				Group rg = resolve_group(solid);
 				LaunchDesc L;
 				prep(rg, L);
-				if (launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidResolve) != cudaSuccess)
+				if (launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidResolve, nullptr) != cudaSuccess)
 					cst = cuda_fail(cudaGetLastError(), "capture resolve");
 			}
 		}
@@ -743,6 +761,32 @@ cvx_status cvx_plan_destroy(cvx_plan* p) {
 	if (p->staging) cudaFreeHost(p->staging);
 	delete p;
 	return CVX_OK;
+}
+
+cvx_status cvx_profile_enable(int on) {
+	g_profile = on != 0;
+	return CVX_OK;
+}
+
+int cvx_profile_collect(const char** names, float* ms, int max_entries) {
+	int n = 0;
+	const char* pending = nullptr;
+	cudaEvent_t prev = nullptr;
+	for (const Mark& m : t_marks) {
+		if (cudaEventSynchronize(m.ev) != cudaSuccess) break;
+		if (m.name && prev && n < max_entries) {
+			float t = 0.0f;
+			cudaEventElapsedTime(&t, prev, m.ev);
+			if (names) names[n] = m.name;
+			if (ms) ms[n] = t;
+			n++;
+		}
+		(void)pending;
+		prev = m.ev;
+	}
+	for (const Mark& m : t_marks) cudaEventDestroy(m.ev);
+	t_marks.clear();
+	return n;
 }
 
 cvx_status cvx_get_tuning(int device, cvx_tuning* out) {

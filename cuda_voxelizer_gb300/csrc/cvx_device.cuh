@@ -16,19 +16,26 @@
 namespace cvx {
 
 // ------------------------------------------------------------------------------------------------
-// Fused-multiply-add pattern of the reference kernels (as compiled by nvcc --fmad=true).
-// Values follow the oracle's ovx_mode (oracle/cvx_oracle.c): 1 = the first product of a*b+c*d is
-// fused, fma(a,b,c*d); 2 = the second, fma(c,d,a*b).
+// Fused-multiply-add pattern of the reference kernels as nvcc (--fmad=true) compiles them for
+// sm_103a.  Values: 0 = no fusion, a*b and c*d rounded separately; 1 = the first product is fused,
+// fma(a, b, c*d); 2 = the second, fma(c, d, a*b) (for a*b - c*d: fma(a,b,-(c*d)) / fma(-c,d,a*b)).
+// Pinned empirically against the reference kernels compiled from their own sources (bit-exact
+// tables on millions of near-tie voxels; source level reasons in parentheses):
 struct RefFma {
-	static constexpr int cross = 1;    // helper_math cross(): a.y*b.z - a.z*b.y -> fma(a.y,b.z,-(a.z*b.y))
-	static constexpr int dot3 = 1;     // helper_math dot(float3): fma(z,z',fma(x,x',y*y'))
-	static constexpr int dot2 = 1;     // helper_math dot(float2) in the triangle setup: fma(x,x',y*y')
-	static constexpr int plane = 1;    // per-voxel dot(n,p): 1 fma(nz,pz,fma(nx,px,ny*py)); 2 fma(nx,px,ny*py)+nz*pz
-	static constexpr int edge_xy = 1;  // per-voxel dot(n_xy_e, p_xy)
-	static constexpr int edge_yz = 1;  // per-voxel dot(n_yz_e, p_yz)
-	static constexpr int edge_zx = 1;  // per-voxel dot(n_zx_e, p_zx)
-	static constexpr int ccw = 1;      // solid checkCCW / check_point_triangle a*b-c*d
-	static constexpr int getx = 1;     // solid get_x_coordinate n.y*A + n.z*B
+	static constexpr int cross = 1;    // helper_math cross() in normalize(cross(e0, e1))
+	static constexpr int dot3 = 1;     // dot(c, c) inside normalize: fma(z,z',fma(x,x',y*y'))
+	static constexpr int dot3d = 1;    // d1, d2 = dot(n, c - v0), dot(n, delta_p - c - v0)
+	static constexpr int dot2_xy = 2;  // setup dot(n_xy_e, v.xy): n_xy_e.x = -1.0f*e.y is a negation,
+	static constexpr int dot2_yz = 2;  //   so its product is not the one fused; same for n_yz_e,
+	static constexpr int dot2_zx = 2;  //   n_zx_e (src/voxelize.cu:99-133)
+	static constexpr int plane = 2;    // per-voxel dot(n,p): fma(nx,px,ny*py) + nz*pz (the y and z
+	                                   //   products are hoisted out of the x loop before fusion)
+	static constexpr int edge_xy = 1;  // per-voxel dot(n_xy_e, p_xy): fma(a.x, px, a.y*py)
+	static constexpr int edge_yz = 1;  // per-voxel dot(n_yz_e, p_yz): fma(a.x, py, a.y*pz)
+	static constexpr int edge_zx = 2;  // per-voxel dot(n_zx_e, p_zx): fma(a.y, px, a.x*pz) (pz term hoisted)
+	static constexpr int ccw = 2;      // solid checkCCW: e0.x*e1.y - e1.x*e0.y -> fma(-e1.x, e0.y, e0.x*e1.y)
+	static constexpr int pt = 1;       // solid check_point_triangle t1..t3: fma(a, b, -(c*d))
+	static constexpr int getx = 1;     // solid get_x_coordinate: fma(n.y, A, n.z*B)
 };
 
 template <int P>

@@ -24,15 +24,24 @@ struct Tune {
 	uint32_t small_cols = 32;   // solid: columns at or below which a triangle stays in its thread
 };
 
+// Optional per-kernel timing: mark(name) records an event on the stream after the named kernel
+// (and once with name == nullptr before the first kernel of a sequence).
+struct Prof {
+	void (*mark)(void* ctx, const char* name, cudaStream_t s);
+	void* ctx;
+	void operator()(const char* name, cudaStream_t s) const { mark(ctx, name, s); }
+};
+
 // Surface launch sequence: classify + cooperative rows.  Counters must be zero.
-cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s);
+cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s, const Prof* prof);
 int surf_rows_blocks_per_sm();
 
 // Solid launch sequence.  kSolidToggles: classify + cooperative columns (counters must be zero);
 // kSolidResolve: prefix-XOR resolve into the tables (+ Morton transcode).  Every job's flips table
 // must be zero before the toggles and is zero again after the resolve.
 enum : unsigned { kSolidToggles = 1u, kSolidResolve = 2u };
-cudaError_t launch_solid(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases);
+cudaError_t launch_solid(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases,
+                         const Prof* prof);
 int solid_cols_blocks_per_sm();
 
 // Resolve-unit bookkeeping of a solid job: rows per unit and units per job.

@@ -94,9 +94,9 @@ __device__ __forceinline__ bool column_hit(const SolidTri& S, const float* unit,
 	const float PBx = __fsub_rn(px, S.bx), PBy = __fsub_rn(py, S.by);
 	const float PCx = __fsub_rn(px, S.cx), PCy = __fsub_rn(py, S.cy);
 	int check;
-	const float t1 = mul_sub<P::ccw>(PAx, PBy, PAy, PBx);
-	const float t2 = mul_sub<P::ccw>(PBx, PCy, PBy, PCx);
-	const float t3 = mul_sub<P::ccw>(PCx, PAy, PCy, PAx);
+	const float t1 = mul_sub<P::pt>(PAx, PBy, PAy, PBx);
+	const float t2 = mul_sub<P::pt>(PBx, PCy, PBy, PCx);
+	const float t3 = mul_sub<P::pt>(PCx, PAy, PCy, PAx);
 	if ((double)fabsf(t1) < kFloatError && __fmul_rn(PAx, PBx) <= 0.0f && __fmul_rn(PAy, PBy) <= 0.0f) check = 1;
 	else if ((double)fabsf(t2) < kFloatError && __fmul_rn(PBx, PCx) <= 0.0f && __fmul_rn(PBy, PCy) <= 0.0f) check = 2;
 	else if ((double)fabsf(t3) < kFloatError && __fmul_rn(PCx, PAx) <= 0.0f && __fmul_rn(PCy, PAy) <= 0.0f) check = 3;
@@ -502,31 +502,39 @@ SolidUnits solid_units(const uint32_t grid[3]) {
 }
 
 template <class P>
-static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases) {
+static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases,
+                                  const Prof* prof) {
 	cudaError_t e = cudaSuccess;
+	if (prof) (*prof)(nullptr, s);
 	if ((phases & kSolidToggles) && L.n_tiles) {
 		solid_classify<P><<<L.n_tiles, kTile, 0, s>>>(L, tune.small_cols);
 		if ((e = cudaGetLastError()) != cudaSuccess) return e;
+		if (prof) (*prof)("solid_classify", s);
 		solid_cols<P><<<cols_grid, kRowsThreads, 0, s>>>(L);
 		if ((e = cudaGetLastError()) != cudaSuccess) return e;
+		if (prof) (*prof)("solid_cols", s);
 	}
 	if (phases & kSolidResolve) {
 		if (L.n_units) {
 			solid_resolve<<<(L.n_units + 7) / 8, 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			if (prof) (*prof)("solid_resolve", s);
 		}
 		if (L.n_mwords) {
 			solid_morton<<<(unsigned)((L.n_mwords + 255) / 256), 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			if (prof) (*prof)("solid_morton", s);
 			solid_zero<<<(L.n_units + 7) / 8, 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			if (prof) (*prof)("solid_zero", s);
 		}
 	}
 	return cudaSuccess;
 }
 
-cudaError_t launch_solid(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases) {
-	return launch_solid_t<RefFma>(L, tune, cols_grid, s, phases);
+cudaError_t launch_solid(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases,
+                         const Prof* prof) {
+	return launch_solid_t<RefFma>(L, tune, cols_grid, s, phases, prof);
 }
 
 int solid_cols_blocks_per_sm() {

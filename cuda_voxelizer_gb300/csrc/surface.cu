@@ -281,17 +281,21 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 // ---- host-side launchers ------------------------------------------------------------------------
 
 template <class P>
-static cudaError_t launch_surface_t(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s) {
+static cudaError_t launch_surface_t(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s,
+                                    const Prof* prof) {
 	if (L.n_tiles == 0) return cudaSuccess;
+	if (prof) (*prof)(nullptr, s);
 	surf_classify<P><<<L.n_tiles, kTile, 0, s>>>(L, tune.small_vox);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
+	if (prof) (*prof)("surf_classify", s);
 	surf_rows<P><<<rows_grid, kRowsThreads, 0, s>>>(L);
+	if (prof) (*prof)("surf_rows", s);
 	return cudaGetLastError();
 }
 
-cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s) {
-	return launch_surface_t<RefFma>(L, tune, rows_grid, s);
+cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s, const Prof* prof) {
+	return launch_surface_t<RefFma>(L, tune, rows_grid, s, prof);
 }
 
 int surf_rows_blocks_per_sm() {

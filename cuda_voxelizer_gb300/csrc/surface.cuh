@@ -26,6 +26,15 @@ struct SurfTri {
 	int bx0, by0, bz0, bx1, by1, bz1;        // clamped grid bbox
 };
 
+// dot(n_e, v) of the setup, a.x*v.x + a.y*v.y, where n_e = (-e.?, e.?) may have been negated
+// (flip < 0).  Pattern 3: second product fused unless flipped, then the first; 4: the opposite.
+template <int P>
+__device__ __forceinline__ float setup_dot(float ax, float vx, float ay, float vy, float flip) {
+	if constexpr (P == 3) return flip < 0.0f ? mul_add<1>(ax, vx, ay, vy) : mul_add<2>(ax, vx, ay, vy);
+	else if constexpr (P == 4) return flip < 0.0f ? mul_add<2>(ax, vx, ay, vy) : mul_add<1>(ax, vx, ay, vy);
+	else return mul_add<P>(ax, vx, ay, vy);
+}
+
 // Triangle setup, src/voxelize.cu:71-133.  `t` holds v0.xyz, v1.xyz, v2.xyz in world space.
 template <class P>
 __device__ __forceinline__ void surf_setup(const float* t, const float* bmin, const float* unit, const uint32_t* grid,
@@ -58,8 +67,8 @@ __device__ __forceinline__ void surf_setup(const float* t, const float* bmin, co
 	const float cxp = S.nx > 0.0f ? unit[0] : 0.0f;
 	const float cyp = S.ny > 0.0f ? unit[1] : 0.0f;
 	const float czp = S.nz > 0.0f ? unit[2] : 0.0f;
-	S.d1 = dot3<P::dot3>(S.nx, S.ny, S.nz, __fsub_rn(cxp, v0x), __fsub_rn(cyp, v0y), __fsub_rn(czp, v0z));
-	S.d2 = dot3<P::dot3>(S.nx, S.ny, S.nz, __fsub_rn(__fsub_rn(unit[0], cxp), v0x),
+	S.d1 = dot3<P::dot3d>(S.nx, S.ny, S.nz, __fsub_rn(cxp, v0x), __fsub_rn(cyp, v0y), __fsub_rn(czp, v0z));
+	S.d2 = dot3<P::dot3d>(S.nx, S.ny, S.nz, __fsub_rn(__fsub_rn(unit[0], cxp), v0x),
 	                     __fsub_rn(__fsub_rn(unit[1], cyp), v0y), __fsub_rn(__fsub_rn(unit[2], czp), v0z));
 
 	// projection tests (:97-133).  n_xy_e = (-e.y, e.x), negated when n.z < 0; d = -dot(n_e, v) +
@@ -78,11 +87,11 @@ __device__ __forceinline__ void surf_setup(const float* t, const float* bmin, co
 		S.exy[i][0] = axy; S.exy[i][1] = bxy;
 		S.eyz[i][0] = ayz; S.eyz[i][1] = byz;
 		S.ezx[i][0] = azx; S.ezx[i][1] = bzx;
-		S.dxy[i] = __fadd_rn(__fadd_rn(-mul_add<P::dot2>(axy, vx[i], bxy, vy[i]), fmaxf(0.0f, __fmul_rn(unit[0], axy))),
+		S.dxy[i] = __fadd_rn(__fadd_rn(-setup_dot<P::dot2_xy>(axy, vx[i], bxy, vy[i], sxy), fmaxf(0.0f, __fmul_rn(unit[0], axy))),
 		                     fmaxf(0.0f, __fmul_rn(unit[1], bxy)));
-		S.dyz[i] = __fadd_rn(__fadd_rn(-mul_add<P::dot2>(ayz, vy[i], byz, vz[i]), fmaxf(0.0f, __fmul_rn(unit[1], ayz))),
+		S.dyz[i] = __fadd_rn(__fadd_rn(-setup_dot<P::dot2_yz>(ayz, vy[i], byz, vz[i], syz), fmaxf(0.0f, __fmul_rn(unit[1], ayz))),
 		                     fmaxf(0.0f, __fmul_rn(unit[2], byz)));
-		S.dzx[i] = __fadd_rn(__fadd_rn(-mul_add<P::dot2>(azx, vz[i], bzx, vx[i]), fmaxf(0.0f, __fmul_rn(unit[0], azx))),
+		S.dzx[i] = __fadd_rn(__fadd_rn(-setup_dot<P::dot2_zx>(azx, vz[i], bzx, vx[i], szx), fmaxf(0.0f, __fmul_rn(unit[0], azx))),
 		                     fmaxf(0.0f, __fmul_rn(unit[2], bzx)));
 	}
 }
@@ -100,7 +109,7 @@ template <class P>
 __device__ __forceinline__ void row_consts(const SurfTri& S, float py, float pz, RowK& K) {
 	K.py = py;
 	K.pz = pz;
-	K.kpl = (P::plane == 3) ? 0.0f : __fmul_rn(S.ny, py);
+	K.kpl = __fmul_rn(S.ny, py);
 	K.kpl2 = __fmul_rn(S.nz, pz);
 #pragma unroll
 	for (int i = 0; i < 3; i++) {
@@ -122,7 +131,8 @@ __device__ __forceinline__ uint32_t fail_bits(const SurfTri& S, const RowK& K, f
 	float s;
 	if constexpr (P::plane == 1) s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.nx, px, K.kpl));
 	else if constexpr (P::plane == 2) s = __fadd_rn(__fmaf_rn(S.nx, px, K.kpl), K.kpl2);
-	else s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.ny, K.py, __fmul_rn(S.nx, px)));
+	else if constexpr (P::plane == 3) s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.ny, K.py, __fmul_rn(S.nx, px)));
+	else s = __fadd_rn(__fadd_rn(__fmul_rn(S.nx, px), K.kpl), K.kpl2);
 	const float a = __fadd_rn(s, S.d1), b = __fadd_rn(s, S.d2);
 	const bool pf = __fmul_rn(a, b) > 0.0f;
 	uint32_t f = (pf && a < 0.0f ? 1u : 0u) | (pf && a > 0.0f ? 2u : 0u);
@@ -130,14 +140,14 @@ __device__ __forceinline__ uint32_t fail_bits(const SurfTri& S, const RowK& K, f
 	for (int i = 0; i < 3; i++) {
 		float v;
 		if constexpr (P::edge_xy == 1) v = __fmaf_rn(S.exy[i][0], px, K.kxy[i]);
-		else v = __fmaf_rn(S.exy[i][1], K.py, __fmul_rn(S.exy[i][0], px));
+		else v = mul_add<P::edge_xy>(S.exy[i][0], px, S.exy[i][1], K.py);
 		f |= (__fadd_rn(v, S.dxy[i]) < 0.0f ? 1u : 0u) << (2 + i);
 	}
 #pragma unroll
 	for (int i = 0; i < 3; i++) {
 		float v;
-		if constexpr (P::edge_zx == 1) v = __fmaf_rn(S.ezx[i][0], K.pz, __fmul_rn(S.ezx[i][1], px));
-		else v = __fmaf_rn(S.ezx[i][1], px, K.kzx[i]);
+		if constexpr (P::edge_zx == 2) v = __fmaf_rn(S.ezx[i][1], px, K.kzx[i]);
+		else v = mul_add<P::edge_zx>(S.ezx[i][0], K.pz, S.ezx[i][1], px);
 		f |= (__fadd_rn(v, S.dzx[i]) < 0.0f ? 1u : 0u) << (5 + i);
 	}
 	return f;

@@ -131,6 +131,20 @@ typedef struct cvx_tuning {
 cvx_status cvx_get_tuning(int device, cvx_tuning* out);
 cvx_status cvx_set_tuning(int device, const cvx_tuning* in);
 
+/* ---- per-kernel timing ---------------------------------------------------------------------- */
+
+/* When enabled, calls made by this host thread record a CUDA event after each engine kernel on
+ * their stream.  cvx_profile_collect waits for those events, writes up to max_entries (kernel
+ * name, milliseconds) pairs in launch order and forgets them.  Names are static strings. */
+cvx_status cvx_profile_enable(int on);
+int cvx_profile_collect(const char** names, float* ms, int max_entries);
+
+/* ---- peak measurement for the roofline ------------------------------------------------------- */
+
+/* 32-bit global atomicOr per second into d_table (words long): pattern 0 scattered lanes,
+ * 1 one 128-byte line per warp, 2 eight consecutive words per lane.  Synchronous. */
+double cvx_microbench_atomic_or(uint32_t* d_table, uint64_t words, int pattern, uint32_t blocks, uint32_t iters);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
