@@ -43,8 +43,8 @@ SAMPLE_FRACTION = 32
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=400)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["engine", "reference"], default="engine")
     p.add_argument("--no-extras", action="store_true", help="skip the soup / batch side measurements")
     return p.parse_args()
@@ -88,23 +88,35 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        """Starts sampling and returns once the first sample has arrived, so that the timed region
+        that follows is covered."""
+        self.lines = []
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            first = self.proc.stdout.readline()
+            if first:
+                self.lines.append(first)
+            self.reader = threading.Thread(target=self._drain, daemon=True)
+            self.reader.start()
         except OSError:
             self.proc = None
         return self
 
+    def _drain(self):
+        for line in self.proc.stdout:
+            self.lines.append(line)
+
     def __exit__(self, *a):
-        self.out = ""
         if self.proc:
             self.proc.terminate()
             try:
-                self.out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                self.out, _ = self.proc.communicate()
+            self.reader.join(timeout=5)
+        self.out = "".join(self.lines)
 
     def summary(self):
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
@@ -119,7 +131,7 @@ class ClockSampler:
             except ValueError:
                 continue
             for n, v in zip(names, f[3:7]):
-                if v.lower() == "active":
+                if v.strip().lower() == "active":
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
@@ -151,16 +163,25 @@ def cpu_sample(tris):
 
 
 def time_cpu_reference(info_bytes, sample, threads):
-    """Reference CPU algorithm over the 4 modes on the sample; returns seconds."""
+    """The reference CPU algorithm over the 4 modes on a sample of the mesh (same grid, the
+    sample's triangle count); returns seconds.  Runs the reference's own build where it exists on
+    this host, else the oracle port of it (same structure: OpenMP over triangles, a critical
+    section per bit write)."""
     import oracle
+    info_s = oracle.with_count(info_bytes, sample.shape[0])
+    os.environ["OMP_NUM_THREADS"] = str(threads)
     t0 = time.perf_counter()
     for morton, solid in MODES:
-        oracle.voxelize_omp(info_bytes, sample, morton=morton, solid=solid, threads=threads)
+        if oracle.ref_cpu_available():
+            oracle.ref_cpu_voxelize(info_s, sample, morton=morton, solid=solid)
+        else:
+            oracle.voxelize_omp(info_s, sample, morton=morton, solid=solid, threads=threads)
     return time.perf_counter() - t0
 
 
 def run_reference_arm(args, rank, world):
-    """--impl reference: the reference's CPU implementation (OpenMP) on a bounded sample."""
+    """--impl reference: the reference's CPU implementation (OpenMP) on a bounded sample, sized so
+    that warm-up plus timed steps take about 90 s of CPU time in total."""
     if rank != 0:
         return
     import oracle
@@ -169,21 +190,26 @@ def run_reference_arm(args, rank, world):
     tris = meshgen.icosphere(0, level=8)
     info = bytes(cv.make_voxinfo(tris, 512))
     threads = os.cpu_count() or 1
-    sample = cpu_sample(tris)
     kind = "reference" if oracle.ref_cpu_available() else "port"
+    probe_n = 1024
+    t_probe = max(1e-4, time_cpu_reference(info, np.ascontiguousarray(tris[:probe_n]), threads))
+    per_step = min(10.0, 90.0 / max(1, args.steps + args.warmup))
+    n = int(np.clip(probe_n * per_step / t_probe, 256, tris.shape[0]))
+    sample = np.ascontiguousarray(tris[:n])
     for _ in range(args.warmup):
-        time_cpu_reference(info, sample[: max(1, sample.shape[0] // 8)], threads)
+        time_cpu_reference(info, sample, threads)
     ts = [time_cpu_reference(info, sample, threads) for _ in range(args.steps)]
     sec = float(np.mean(ts))
-    value = 4 * sample.shape[0] / sec / 1e6
+    value = 4 * n / sec / 1e6
+    desc = (f"first {n} of {tris.shape[0]} triangles, 4 modes, OpenMP parallel-for with a critical section per "
+            f"bit ({kind})")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere)",
-            "config": {"workload": "icosphere level 8 (1,310,720 tris) at 512^3, 4 modes; sample 1/32",
-                       "sample_triangles": int(sample.shape[0])},
-            "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": threads, "kind": kind,
-                             "sample": f"first {sample.shape[0]} of 1,310,720 triangles (1/{SAMPLE_FRACTION}), "
-                                       "4 modes, OpenMP parallel-for with a critical section per bit"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced icosphere)",
+            "config": {"workload": "icosphere level 8 (1,310,720 tris) at 512^3; surface+solid x linear+Morton "
+                                   "per step", "gridsize": 512, "triangles": int(tris.shape[0]),
+                       "sample_triangles": n},
+            "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": threads, "kind": kind, "sample": desc},
             "e2e": {"value": value, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -66,16 +66,27 @@ def table_words(info: bytes) -> int:
     return int((int(g[0]) * int(g[1]) * int(g[2]) + 31) // 32)
 
 
-def _soup(tris) -> np.ndarray:
+def _soup(tris, info: bytes | None = None) -> np.ndarray:
     t = np.ascontiguousarray(np.asarray(tris, dtype=np.float32).reshape(-1, 9))
+    if info is not None:
+        n = int(np.frombuffer(info, dtype=np.uint64, count=1, offset=40)[0])
+        if t.shape[0] < n:
+            raise ValueError(f"voxinfo says {n} triangles but only {t.shape[0]} were given")
     return t
+
+
+def with_count(info: bytes, n: int) -> bytes:
+    """The same voxinfo with n_triangles replaced (e.g. for a sample of the mesh)."""
+    b = bytearray(info)
+    b[40:48] = int(n).to_bytes(8, "little")
+    return bytes(b)
 
 
 def voxelize(info: bytes, tris, morton: bool = False, solid: bool = False, mode: OvxMode | None = None,
              table: np.ndarray | None = None) -> np.ndarray:
     """Serial restatement; returns (or ORs/XORs into) a uint32 table of ceil(g^3/32) words."""
     assert len(info) == 64
-    t = _soup(tris)
+    t = _soup(tris, info)
     ib = ctypes.create_string_buffer(bytes(info), 64)
     if table is None:
         table = np.zeros(table_words(info), dtype=np.uint32)
@@ -86,7 +97,7 @@ def voxelize(info: bytes, tris, morton: bool = False, solid: bool = False, mode:
 
 def voxelize_omp(info: bytes, tris, morton: bool = False, solid: bool = False, threads: int = 0) -> np.ndarray:
     """Restatement run like the reference's OpenMP CPU path (parallel for, critical per bit)."""
-    t = _soup(tris)
+    t = _soup(tris, info)
     ib = ctypes.create_string_buffer(bytes(info), 64)
     table = np.zeros(table_words(info), dtype=np.uint32)
     lib().ovx_voxelize_omp(ctypes.addressof(ib), _ptr(t), _ptr(table), int(morton), int(solid), int(threads))
@@ -157,7 +168,7 @@ def ref_cpu_voxelize(info: bytes, tris, morton: bool = False, solid: bool = Fals
     L = ref_cpu_lib()
     if L is None:
         raise RuntimeError("reference CPU build not available on this machine")
-    t = _soup(tris)
+    t = _soup(tris, info)
     ib = ctypes.create_string_buffer(bytes(info), 64)
     table = np.zeros(table_words(info), dtype=np.uint32)
     fn = L.ref_cpu_voxelize_solid if solid else L.ref_cpu_voxelize

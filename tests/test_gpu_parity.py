@@ -269,7 +269,7 @@ def test_caller_workspace_equals_internal(solid):
     td = torch.from_numpy(t.reshape(-1)).cuda()
     ws = torch.empty(cv.workspace_size(info, solid), dtype=torch.uint8, device="cuda")
     a = torch.zeros(cv.table_words(info) + GUARD, dtype=torch.int32, device="cuda")
-    cv.voxelize_ws(info, td, a, ws, morton=False, solid=solid)
+    cv.voxelize_ws(info, td, a, ws, morton_code=False, solid=solid)
     b = run_engine(info, td, False, solid)
     torch.cuda.synchronize()
     assert torch.equal(a, b)
