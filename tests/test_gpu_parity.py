@@ -210,7 +210,7 @@ def test_accumulates_into_existing_table(ref):
     t0 = meshgen.torus(3)
     info0 = info_of(t0, 64)
     td0 = torch.from_numpy(t0.reshape(-1)).cuda()
-    init = torch.randint(-2 ** 31, 2 ** 31 - 1, (cv.table_words(info) + GUARD,), dtype=torch.int32, device="cuda")
+    init = torch.randint(-2 ** 31, 2 ** 31 - 1, (cv.table_words(info0) + GUARD,), dtype=torch.int32, device="cuda")
     for solid in (False, True):
         t, info = for_reference(t0, info0, False, solid)
         td = torch.from_numpy(t.reshape(-1)).cuda() if solid else td0
