@@ -52,6 +52,7 @@ SIGNATURES = {
     "cvx_voxelize_solid": (c_status, [ctypes.POINTER(CvxVoxinfo), vp, vp, ctypes.c_int, vp]),
     "cvx_workspace_size": (u64, [ctypes.POINTER(CvxVoxinfo), ctypes.c_int]),
     "cvx_voxelize_ws": (c_status, [ctypes.POINTER(CvxVoxinfo), vp, vp, ctypes.c_int, ctypes.c_int, vp, u64, vp]),
+    "cvx_voxelize_solid_noalloc": (c_status, [ctypes.POINTER(CvxVoxinfo), vp, vp, ctypes.c_int, vp]),
     "cvx_device_status": (c_status, [vp]),
     "cvx_voxelize_batch": (c_status, [ctypes.POINTER(CvxJob), u32, vp]),
     "cvx_plan_create": (c_status, [ctypes.POINTER(CvxJob), u32, u32, ctypes.POINTER(vp)]),

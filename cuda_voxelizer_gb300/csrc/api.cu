@@ -418,6 +418,8 @@ cvx_status run_internal(std::vector<JobDesc> surf, std::vector<JobDesc> solid, c
 
 }  // namespace
 
+void cvx::set_message(const std::string& m) { g_msg = m; }
+
 // ==== C ABI =======================================================================================
 
 extern "C" {

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <string>
 #include "cvx_device.cuh"
 
 namespace cvx {
@@ -51,5 +52,8 @@ struct SolidUnits {
 	bool aligned;   // gx % 32 == 0: rows start on word boundaries
 };
 SolidUnits solid_units(const uint32_t grid[3]);
+
+// Sets the message returned by cvx_last_error_message() on this host thread.
+void set_message(const std::string& m);
 
 }  // namespace cvx

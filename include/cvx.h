@@ -96,6 +96,18 @@ uint64_t cvx_workspace_size(const cvx_voxinfo* info, int solid);
 cvx_status cvx_voxelize_ws(const cvx_voxinfo* info, const float* d_triangles, uint32_t* d_table, int morton,
                            int solid, void* d_workspace, uint64_t workspace_bytes, cvx_stream_t stream);
 
+/* Solid voxelization that allocates nothing (no counterpart in the reference).  For callers that must
+ * not allocate device memory while voxelizing -- e.g. per-frame code that budgets all GPU memory at
+ * start-up (an allocation mid-frame can stall the device or fail under memory pressure), or hosts
+ * whose memory policy forbids driver allocations.  Same result as cvx_voxelize_solid.  Its scratch
+ * is a fixed 4 MiB array inside the library (held by every GPU that loads it until exit), so the
+ * grid may hold at most 2^24 voxels (e.g. 256^3); larger grids return CVX_ERR_INVALID_VALUE.  The
+ * first call on a device looks up that array's device address and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race, so issue them one at a
+ * time. */
+cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const float* d_triangles, uint32_t* d_table,
+                                      int morton, cvx_stream_t stream);
+
 /* Synchronizes `stream` and reports device-side checks of the last calls made on it through the
  * library-owned scratch: CVX_OK, or CVX_ERR_DEVICE_CHECK (a queue overflow or a timed-out copy). */
 cvx_status cvx_device_status(cvx_stream_t stream);
