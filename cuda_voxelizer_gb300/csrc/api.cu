@@ -228,13 +228,12 @@ struct Group {
 	std::vector<JobDesc> jobs;
 	uint64_t tris = 0;
 	uint32_t tiles = 0, units = 0;
-	uint64_t mwords = 0;
-	uint64_t flip_words = 0;
+	uint64_t mwords = 0, mbricks = 0;
 };
 
 void finish_group(Group& g, bool solid) {
 	uint32_t tile = 0, unit = 0;
-	uint64_t mw = 0;
+	uint64_t mw = 0, mb = 0;
 	g.tris = 0;
 	for (JobDesc& j : g.jobs) {
 		j.tile_begin = tile;
@@ -244,12 +243,18 @@ void finish_group(Group& g, bool solid) {
 			j.unit_begin = unit;
 			unit += (uint32_t)solid_units(j.grid).units;
 			j.mword_begin = mw;
-			if (j.flags & JOB_MORTON) mw += ((uint64_t)j.grid[0] * j.grid[1] * j.grid[2] + 31) / 32;
+			j.mbrick_begin = mb;
+			const uint64_t vox = (uint64_t)j.grid[0] * j.grid[1] * j.grid[2];
+			if (j.flags & JOB_MORTON) {
+				if (j.grid[0] >= 32) mb += vox >> 15;  // 32^3 voxels per brick
+				else mw += (vox + 31) / 32;
+			}
 		}
 	}
 	g.tiles = tile;
 	g.units = unit;
 	g.mwords = mw;
+	g.mbricks = mb;
 }
 
 // Split jobs of one mode into launch groups of fewer than kMaxTriPerLaunch triangles.  A job above
@@ -315,6 +320,7 @@ struct Runner {
 		L.n_tiles = g.tiles;
 		L.n_units = g.units;
 		L.n_mwords = g.mwords;
+		L.n_mbricks = g.mbricks;
 		L.scr.ctr = reinterpret_cast<Counters*>(rec);
 		const RecLayout lay = rec_layout(cap, 0);
 		L.scr.big = reinterpret_cast<BigRec*>(rec + lay.big);
@@ -694,6 +700,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 			L.n_tiles = g.tiles;
 			L.n_units = g.units;
 			L.n_mwords = g.mwords;
+			L.n_mbricks = g.mbricks;
 			L.scr.ctr = reinterpret_cast<Counters*>(p->rec);
 			const RecLayout l0 = rec_layout(cap, 0);
 			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(p->rec) + l0.big);

@@ -75,7 +75,8 @@ struct JobDesc {
 	uint32_t flags;        // JOB_MORTON | JOB_SOLID
 	uint32_t tile_begin;   // first triangle tile of this job in the launch's tile space
 	uint32_t unit_begin;   // solid: first resolve unit of this job in the launch's unit space
-	uint64_t mword_begin;  // solid Morton: first Morton word of this job in the launch's word space
+	uint64_t mword_begin;  // solid Morton, g < 32: first Morton word in the launch's word space
+	uint64_t mbrick_begin; // solid Morton, g >= 32: first 32^3 brick in the launch's brick space
 };
 
 // Work-queue records written by the classify kernels and consumed by the cooperative kernels.
@@ -116,8 +117,8 @@ struct LaunchDesc {
 	uint32_t n_jobs;
 	uint32_t n_tiles;      // total triangle tiles over all jobs
 	uint32_t n_units;      // solid resolve units over all jobs
-	uint32_t pad;
-	uint64_t n_mwords;     // solid Morton words over all jobs
+	uint64_t n_mwords;     // Morton words of solid Morton jobs with g < 32
+	uint64_t n_mbricks;    // 32^3 bricks of solid Morton jobs with g >= 32
 	Scratch scr;
 };
 

@@ -165,6 +165,9 @@ extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const 
 	L.single.n_tri = 0;
 	L.n_tiles = 0;
 	L.n_units = (uint32_t)su.units;
-	L.n_mwords = morton ? words : 0;
+	if (morton) {
+		if (g0 >= 32) L.n_mbricks = (g0 * g1 * g2) >> 15;
+		else L.n_mwords = words;
+	}
 	return cuda_status(launch_solid(L, tune, cols_grid, s, kSolidResolve, nullptr), "solid resolve");
 }

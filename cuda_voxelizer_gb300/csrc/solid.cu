@@ -24,6 +24,22 @@ namespace {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr double kFloatError = 0.000001;  // src/voxelize_solid.cu:13 (a double literal)
+// For a float f, (double)f < 0.000001 exactly when f <= 0x1.0c6f7ap-20f, the largest float below the
+// double 1e-6 (floats are exact in double, and 0x1.0c6f7ap-20 < 1e-6 < its successor).
+constexpr float kFloatErrorBelow = 0x1.0c6f7ap-20f;
+
+// floor((double)q - 0.5) and ceil(...) for a float q: q - 0.5f is exact in float when |q| < 2^22
+// (its ulp is at most 0.5 there), so float floor/ceil give the double result; else use double.
+__device__ __forceinline__ float floor_half(float q) {
+	return fabsf(q) < 4194304.0f ? floorf(__fsub_rn(q, 0.5f)) : (float)floor((double)q - 0.5);
+}
+__device__ __forceinline__ float ceil_half(float q) {
+	return fabsf(q) < 4194304.0f ? ceilf(__fsub_rn(q, 0.5f)) : (float)ceil((double)q - 0.5);
+}
+// int((double)q - 0.5) (truncation, saturating as cvt.rzi.s32.f64 does)
+__device__ __forceinline__ int trunc_half(float q) {
+	return fabsf(q) < 4194304.0f ? __float2int_rz(__fsub_rn(q, 0.5f)) : __double2int_rz((double)q - 0.5);
+}
 
 struct SolidTri {
 	float nx, ny, nz;
@@ -50,7 +66,7 @@ __device__ __forceinline__ void solid_setup(const float* t, const float* bmin, c
 	S.ny = __fmul_rn(cy, inv);
 	S.nz = __fmul_rn(cz, inv);
 	S.v0x = v0x; S.v0y = v0y; S.v0z = v0z;
-	S.skip = (double)fabsf(S.nx) < kFloatError;  // :92 (the thread returns)
+	S.skip = fabsf(S.nx) <= kFloatErrorBelow;  // :92, (double)|n.x| < 1e-6 (the thread returns)
 	// YZ projection, made counter-clockwise (:95-105; checkCCW :55-64)
 	float ax = v0y, ay = v0z, bx = v1y, by = v1z, qx = v2y, qy = v2z;
 	const float ccw = mul_sub<P::ccw>(__fsub_rn(bx, ax), __fsub_rn(qy, ay), __fsub_rn(qx, ax), __fsub_rn(by, ay));
@@ -64,10 +80,10 @@ __device__ __forceinline__ void solid_setup(const float* t, const float* bmin, c
 	// table or into neighbouring rows).
 	const float mxy = fmaxf(ax, fmaxf(bx, qx)), mxz = fmaxf(ay, fmaxf(by, qy));
 	const float mny = fminf(ax, fminf(bx, qx)), mnz = fminf(ay, fminf(by, qy));
-	const float gmaxy = (float)floor((double)__fdiv_rn(mxy, unit[1]) - 0.5);
-	const float gmaxz = (float)floor((double)__fdiv_rn(mxz, unit[2]) - 0.5);
-	const float gminy = (float)ceil((double)__fdiv_rn(mny, unit[1]) - 0.5);
-	const float gminz = (float)ceil((double)__fdiv_rn(mnz, unit[2]) - 0.5);
+	const float gmaxy = floor_half(__fdiv_rn(mxy, unit[1]));
+	const float gmaxz = floor_half(__fdiv_rn(mxz, unit[2]));
+	const float gminy = ceil_half(__fdiv_rn(mny, unit[1]));
+	const float gminz = ceil_half(__fdiv_rn(mnz, unit[2]));
 	int y0 = __float2int_rz(gminy), z0 = __float2int_rz(gminz);
 	// last integer y with (float)y <= gmax (gmax holds an integer value, or is not finite)
 	int y1 = gmaxy >= 2147483520.0f ? 2147483647 : (gmaxy >= -2147483648.0f ? (int)gmaxy : (-2147483647 - 1));
@@ -97,9 +113,9 @@ __device__ __forceinline__ bool column_hit(const SolidTri& S, const float* unit,
 	const float t1 = mul_sub<P::pt>(PAx, PBy, PAy, PBx);
 	const float t2 = mul_sub<P::pt>(PBx, PCy, PBy, PCx);
 	const float t3 = mul_sub<P::pt>(PCx, PAy, PCy, PAx);
-	if ((double)fabsf(t1) < kFloatError && __fmul_rn(PAx, PBx) <= 0.0f && __fmul_rn(PAy, PBy) <= 0.0f) check = 1;
-	else if ((double)fabsf(t2) < kFloatError && __fmul_rn(PBx, PCx) <= 0.0f && __fmul_rn(PBy, PCy) <= 0.0f) check = 2;
-	else if ((double)fabsf(t3) < kFloatError && __fmul_rn(PCx, PAx) <= 0.0f && __fmul_rn(PCy, PAy) <= 0.0f) check = 3;
+	if (fabsf(t1) <= kFloatErrorBelow && __fmul_rn(PAx, PBx) <= 0.0f && __fmul_rn(PAy, PBy) <= 0.0f) check = 1;
+	else if (fabsf(t2) <= kFloatErrorBelow && __fmul_rn(PBx, PCx) <= 0.0f && __fmul_rn(PBy, PCy) <= 0.0f) check = 2;
+	else if (fabsf(t3) <= kFloatErrorBelow && __fmul_rn(PCx, PAx) <= 0.0f && __fmul_rn(PCy, PAy) <= 0.0f) check = 3;
 	else if (__fmul_rn(t1, t2) > 0.0f && __fmul_rn(t1, t3) > 0.0f) check = 0;
 	else check = -1;
 	const bool in = (check == 1 && top_left(S.ax, S.ay, S.bx, S.by)) || (check == 2 && top_left(S.bx, S.by, S.cx, S.cy)) ||
@@ -108,7 +124,7 @@ __device__ __forceinline__ bool column_hit(const SolidTri& S, const float* unit,
 	// get_x_coordinate (:49-52): -(n.y*(p.x - v0.y) + n.z*(p.y - v0.z)) / n.x + v0.x
 	const float m = mul_add<P::getx>(S.ny, __fsub_rn(px, S.v0y), S.nz, __fsub_rn(py, S.v0z));
 	const float xh = __fadd_rn(__fdiv_rn(-m, S.nx), S.v0x);
-	xmax = __double2int_rz((double)__fdiv_rn(xh, unit[0]) - 0.5);  // int(... / unit.x - 0.5)
+	xmax = trunc_half(__fdiv_rn(xh, unit[0]));  // int(... / unit.x - 0.5), the 0.5 a double
 	return true;
 }
 
@@ -179,9 +195,48 @@ __device__ __forceinline__ void stage_tile(const LaunchDesc& L, const float* src
 	__syncthreads();
 }
 
+// A small triangle's solid setup parked in shared memory between the classify phases (16 words).
+struct SmallSolid {
+	float nx, ny, nz, v0x, v0y, v0z, ax, ay, bx, by, cx, cy;
+	int y0, z0;
+	uint32_t ext;  // (y1 - y0) | (z1 - z0) << 16
+	uint32_t pad;
+};
+
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	uint32_t incl = v;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		const uint32_t u = __shfl_up_sync(FULL, incl, d);
+		if (lane >= (uint32_t)d) incl += u;
+	}
+	if (lane == 31) s_warp[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		uint32_t w = lane < kTile / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t u = __shfl_up_sync(FULL, w, d);
+			if (lane >= (uint32_t)d) w += u;
+		}
+		if (lane < kTile / 32) s_warp[lane] = w;
+	}
+	__syncthreads();
+	*total = s_warp[kTile / 32 - 1];
+	return (warp ? s_warp[warp - 1] : 0u) + incl - v;
+}
+
+// Phase 1: one thread per triangle (setup, classify, queue the big ones, park the small ones).
+// Phase 2: the columns of all small triangles of the tile, one (triangle, column) item per thread.
 template <class P>
 __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_cols) {
-	__shared__ __align__(16) float s_tri[kTile * 9];
+	__shared__ __align__(16) union {
+		float tri[kTile * 9];
+		SmallSolid small[kTile];
+	} sm;
+	__shared__ uint32_t s_off[kTile + 1];
+	__shared__ uint32_t s_warp[kTile / 32];
 	__shared__ __align__(8) uint64_t s_bar;
 	const uint32_t tile = blockIdx.x;
 	const uint32_t j = job_of_tile(L, tile);
@@ -194,25 +249,29 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 	uint32_t* flips = J.flips;
 	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
 	const uint32_t cnt = (uint32_t)umin64((uint64_t)kTile, n - t0);
-	stage_tile(L, J.tris + t0 * 9, cnt, s_tri, &s_bar);
+	stage_tile(L, J.tris + t0 * 9, cnt, sm.tri, &s_bar);
 
 	const uint32_t lane = threadIdx.x & 31u;
-	bool is_mid = false, is_big = false;
-	uint32_t n_items = 0;
-	if (threadIdx.x < cnt) {
-		float t[9];
+	const bool valid = threadIdx.x < cnt;
+	float t[9];
 #pragma unroll
-		for (int k = 0; k < 9; k++) t[k] = s_tri[threadIdx.x * 9 + k];
+	for (int k = 0; k < 9; k++) t[k] = valid ? sm.tri[threadIdx.x * 9 + k] : 0.0f;
+	__syncthreads();
+
+	bool is_mid = false, is_big = false;
+	uint32_t n_items = 0, n_cols = 0;
+	if (valid) {
 		SolidTri S;
 		solid_setup<P>(t, bmin, unit, grid, S);
 		if (!S.skip && S.y0 <= S.y1 && S.z0 <= S.z1) {
 			const uint64_t ncols = (uint64_t)(S.y1 - S.y0 + 1) * (uint64_t)(S.z1 - S.z0 + 1);
-			if (ncols <= small_cols) {
-				for (int y = S.y0; y <= S.y1; y++)
-					for (int z = S.z0; z <= S.z1; z++) {
-						int xmax;
-						if (column_hit<P>(S, unit, y, z, xmax)) record_hit(flips, grid, morton, y, z, xmax);
-					}
+			if (ncols <= small_cols && S.y1 - S.y0 < 65536 && S.z1 - S.z0 < 65536) {
+				SmallSolid& o = sm.small[threadIdx.x];
+				o.nx = S.nx; o.ny = S.ny; o.nz = S.nz; o.v0x = S.v0x; o.v0y = S.v0y; o.v0z = S.v0z;
+				o.ax = S.ax; o.ay = S.ay; o.bx = S.bx; o.by = S.by; o.cx = S.cx; o.cy = S.cy;
+				o.y0 = S.y0; o.z0 = S.z0;
+				o.ext = (uint32_t)(S.y1 - S.y0) | ((uint32_t)(S.z1 - S.z0) << 16);
+				n_cols = (uint32_t)ncols;
 			} else {
 				const uint64_t it = (ncols + kColsPerItem - 1) / kColsPerItem;
 				n_items = (uint32_t)umin64(it, 0xFFFFFFu);
@@ -256,6 +315,29 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 				set_error(L, kErrQueueOverflow);
 		}
 	}
+
+	// Phase 2: columns of the small triangles (src/voxelize_solid.cu:115-139).
+	uint32_t total_cols = 0;
+	const uint32_t off = block_scan(n_cols, s_warp, &total_cols);
+	s_off[threadIdx.x] = off;
+	if (threadIdx.x == kTile - 1) s_off[kTile] = total_cols;
+	__syncthreads();
+	for (uint32_t k = threadIdx.x; k < total_cols; k += kTile) {
+		uint32_t lo = 0, hi = kTile;
+		while (hi - lo > 1) {
+			const uint32_t mid = (lo + hi) >> 1;
+			if (s_off[mid] <= k) lo = mid; else hi = mid;
+		}
+		const SmallSolid& o = sm.small[lo];
+		SolidTri S;
+		S.nx = o.nx; S.ny = o.ny; S.nz = o.nz; S.v0x = o.v0x; S.v0y = o.v0y; S.v0z = o.v0z;
+		S.ax = o.ax; S.ay = o.ay; S.bx = o.bx; S.by = o.by; S.cx = o.cx; S.cy = o.cy;
+		const uint32_t c = k - s_off[lo];
+		const uint32_t nzc = (o.ext >> 16) + 1u;
+		const int y = o.y0 + (int)(c / nzc), z = o.z0 + (int)(c % nzc);
+		int xmax;
+		if (column_hit<P>(S, unit, y, z, xmax)) record_hit(flips, grid, morton, y, z, xmax);
+	}
 }
 
 template <class P>
@@ -267,6 +349,9 @@ __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant
 	const uint64_t n_big_items = bigc & kBigItemMask;
 	const uint32_t n_mid = min(*reinterpret_cast<volatile unsigned*>(&C->mid), L.scr.cap);
 	const uint64_t total = n_big_items + n_mid;
+	// Warps beyond the number of queued items have nothing to claim: they leave without touching
+	// the ticket counter (all of them do when only small triangles were queued).
+	if ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) >= total) return;
 	for (;;) {
 		unsigned long long tk = 0;
 		if (lane == 0) tk = atomicAdd(&C->ticket, 1ull);
@@ -313,7 +398,14 @@ __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant
 		const uint64_t c0 = (uint64_t)chunk * kColsPerItem;
 		const uint64_t c1 = umin64(ncols, c0 + kColsPerItem);
 		for (uint64_t c = c0 + lane; c < c1; c += 32) {
-			const int y = S.y0 + (int)(c / nzc), z = S.z0 + (int)(c % nzc);
+			int y, z;
+			if (c1 <= 0xFFFFFFFFull) {
+				y = S.y0 + (int)((uint32_t)c / (uint32_t)nzc);
+				z = S.z0 + (int)((uint32_t)c % (uint32_t)nzc);
+			} else {
+				y = S.y0 + (int)(c / nzc);
+				z = S.z0 + (int)(c % nzc);
+			}
 			int xmax;
 			if (column_hit<P>(S, unit, y, z, xmax)) record_hit(J.flips, grid, morton, y, z, xmax);
 		}
@@ -343,18 +435,22 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 	uint32_t* dest = J.table;
 	const uint64_t u = unit_id - J.unit_begin;
 	if (gx % 32 == 0) {
-		const uint64_t wpr = gx >> 5;
-		const uint64_t rpu = wpr >= 1024 ? 1 : 1024 / wpr;
-		const uint64_t r0 = u * rpu, r1 = min(rows, r0 + rpu);
+		// 32-bit arithmetic only (64-bit division is a slow software routine): gx <= 2^22, so a
+		// row has at most 2^17 words.  A unit is one 32-word window when rows fit in it.
+		const uint32_t wpr = (uint32_t)(gx >> 5);
+		const uint32_t rpu = wpr >= 32 ? 1u : 32u / wpr;
+		const uint64_t r0 = u * rpu, r1 = umin64(rows, r0 + rpu);
 		const uint64_t wbeg = r0 * wpr, wend = r1 * wpr;
+		const bool pow2 = (wpr & (wpr - 1)) == 0;
 		uint32_t carry = 0;
 		for (uint64_t wb = wbeg; wb < wend; wb += 32) {
 			const uint64_t w = wb + lane;
 			const bool active = w < wend;
 			const uint32_t t = active ? flips[w] : 0u;
 			const uint32_t x = __popc(t) & 1u;
+			const uint32_t off = (uint32_t)(wb - wbeg) + lane;
 			uint32_t v = x;
-			bool f = active && ((w - wbeg) % wpr == 0);
+			bool f = active && (pow2 ? (off & (wpr - 1)) == 0 : off % wpr == 0);
 #pragma unroll
 			for (int d = 1; d < 32; d <<= 1) {
 				const uint32_t uv = __shfl_up_sync(FULL, v, d);
@@ -385,16 +481,20 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 			while (b) { uint64_t r = a % b; a = b; b = r; }
 			p = 32 / a;
 		}
-		const uint64_t r0 = u * p, r1 = min(rows, r0 + p);
+		const uint64_t r0 = u * p, r1 = umin64(rows, r0 + p);
 		const uint64_t b0 = r0 * g, b1 = r1 * g;
 		uint32_t carry = 0;
+		uint64_t next_row = b0;  // bit index of the next row start
 		for (uint64_t w = b0 >> 5; (w << 5) < b1; w++) {
 			const uint32_t t = flips[w];
 			uint32_t res = 0;
 			for (uint32_t k = 0; k < 32; k++) {
 				const uint64_t b = (w << 5) + k;
 				if (b >= b1) break;
-				if (b % g == 0) carry = 0;
+				if (b == next_row) {
+					carry = 0;
+					next_row += g;
+				}
 				carry ^= (t >> (31 - k)) & 1u;
 				res |= carry << (31 - k);
 			}
@@ -417,8 +517,59 @@ __device__ __forceinline__ uint32_t compact3(uint64_t v) {
 	return (uint32_t)v;
 }
 
-// Morton jobs: XOR the resolved linear bits into Morton order, one Morton word per thread.
-__global__ void __launch_bounds__(256) solid_morton(const __grid_constant__ LaunchDesc L) {
+// Morton bit mask of a 4-bit row nibble (x = 4X'..4X'+3 in MSB-first order: nibble bit 3 is dx = 0)
+// for dy = dz = 0.  In a Morton word the code offset of (dx, dy, dz) is
+// (dx&1) | (dy&1)<<1 | dz<<2 | (dx>>1)<<3 | (dy>>1)<<4, and bits are MSB first, so other (dy, dz)
+// shift the mask right by 2*(dy&1) + 4*dz + 16*(dy>>1).
+__device__ __forceinline__ uint32_t nibble_mask(uint32_t nib) {
+	uint32_t m = 0;
+	if (nib & 8u) m |= 0x80000000u;         // dx = 0: offset 0
+	if (nib & 4u) m |= 0x80000000u >> 1;    // dx = 1: offset 1
+	if (nib & 2u) m |= 0x80000000u >> 8;    // dx = 2: offset 8
+	if (nib & 1u) m |= 0x80000000u >> 9;    // dx = 3: offset 9
+	return m;
+}
+
+// Morton jobs with g >= 32: one CTA per Morton-aligned 32^3 brick (1,024 consecutive Morton words).
+// The brick's 32 x 32 resolved row words (32 x-bits each) are staged in shared memory and cleared
+// in the flip table (this CTA is their only reader), then each Morton word is assembled from
+// eight 4-bit row nibbles and XORed into the table with coalesced accesses.
+__global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant__ LaunchDesc L) {
+	__shared__ uint32_t s_rows[32 * 32];  // [z][y] word of x-bits of the brick
+	const uint64_t brick = blockIdx.x;
+	const uint32_t j = job_search(L, brick, [](const JobDesc& d) { return d.mbrick_begin; });
+	const JobDesc& J = job_at(L, j);
+	const uint64_t g = J.grid[0];
+	const uint64_t b = brick - J.mbrick_begin;             // brick index within the job
+	const uint64_t bx = compact3(b), by = compact3(b >> 1), bz = compact3(b >> 2);
+	uint32_t* flips = J.flips;
+	for (uint32_t i = threadIdx.x; i < 1024; i += 256) {
+		const uint64_t z = bz * 32 + (i >> 5), y = by * 32 + (i & 31);
+		const uint64_t w = ((z * g + y) * g + bx * 32) >> 5;
+		const uint32_t v = flips[w];
+		s_rows[i] = v;
+		if (v) flips[w] = 0u;
+	}
+	__syncthreads();
+	uint32_t* dest = J.table + (b << 10);
+	for (uint32_t m = threadIdx.x; m < 1024; m += 256) {
+		// local Morton word m covers x' = 4X.., y' = 4Y.., z' = 2Z.. of the brick
+		const uint32_t X = compact3(m >> 1), Y = compact3(m >> 2), Z = compact3(m);
+		uint32_t out = 0;
+#pragma unroll
+		for (uint32_t dz = 0; dz < 2; dz++)
+#pragma unroll
+			for (uint32_t dy = 0; dy < 4; dy++) {
+				const uint32_t row = s_rows[(2 * Z + dz) * 32 + 4 * Y + dy];
+				const uint32_t nib = (row >> (28u - 4u * X)) & 0xFu;
+				out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
+			}
+		if (out) dest[m] ^= out;
+	}
+}
+
+// Morton jobs with g < 32: one Morton word per thread, 32 codes decoded one by one.
+__global__ void __launch_bounds__(256) solid_morton_small(const __grid_constant__ LaunchDesc L) {
 	const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
 	if (idx >= L.n_mwords) return;
 	const uint32_t j = job_search(L, idx, [](const JobDesc& d) { return d.mword_begin; });
@@ -427,32 +578,13 @@ __global__ void __launch_bounds__(256) solid_morton(const __grid_constant__ Laun
 	const uint64_t g = J.grid[0];
 	const uint32_t* flips = J.flips;
 	uint32_t out = 0;
-	if (g >= 32) {
-		// the word holds a 4x4x2 brick: x = 4X+dx, y = 4Y+dy, z = 2Z+dz
-		const uint64_t X = compact3(m >> 1), Y = compact3(m >> 2), Z = compact3(m);
-		const uint64_t x0 = 4 * X;
-#pragma unroll
-		for (uint32_t dz = 0; dz < 2; dz++)
-#pragma unroll
-			for (uint32_t dy = 0; dy < 4; dy++) {
-				const uint64_t row = (2 * Z + dz) * g + (4 * Y + dy);
-				const uint64_t lin = row * g + x0;
-				const uint32_t nib = (flips[lin >> 5] >> (28u - (uint32_t)(lin & 31u))) & 0xFu;
-#pragma unroll
-				for (uint32_t dx = 0; dx < 4; dx++) {
-					const uint32_t o = (dx & 1u) | ((dy & 1u) << 1) | (dz << 2) | ((dx >> 1) << 3) | ((dy >> 1) << 4);
-					out |= ((nib >> (3u - dx)) & 1u) << (31u - o);
-				}
-			}
-	} else {
-		const uint64_t total = g * g * g;
-		for (uint32_t i = 0; i < 32; i++) {
-			const uint64_t c = m * 32 + i;
-			if (c >= total) break;
-			const uint64_t x = compact3(c), y = compact3(c >> 1), z = compact3(c >> 2);
-			const uint64_t lin = x + g * (y + g * z);
-			out |= ((flips[lin >> 5] >> (31u - (uint32_t)(lin & 31u))) & 1u) << (31u - i);
-		}
+	const uint64_t total = g * g * g;
+	for (uint32_t i = 0; i < 32; i++) {
+		const uint64_t c = m * 32 + i;
+		if (c >= total) break;
+		const uint64_t x = compact3(c), y = compact3(c >> 1), z = compact3(c >> 2);
+		const uint64_t lin = x + g * (y + g * z);
+		out |= ((flips[lin >> 5] >> (31u - (uint32_t)(lin & 31u))) & 1u) << (31u - i);
 	}
 	if (out) J.table[m] ^= out;
 }
@@ -464,13 +596,13 @@ __global__ void __launch_bounds__(256) solid_zero(const __grid_constant__ Launch
 	if (unit_id >= L.n_units) return;
 	const uint32_t j = job_search(L, unit_id, [](const JobDesc& d) { return (uint64_t)d.unit_begin; });
 	const JobDesc& J = job_at(L, j);
-	if (!(J.flags & JOB_MORTON)) return;
+	if (!(J.flags & JOB_MORTON) || J.grid[0] >= 32) return;  // bricks clear their own words
 	const uint64_t gx = J.grid[0];
 	const uint64_t rows = (uint64_t)J.grid[1] * J.grid[2];
 	uint64_t rpu;
 	if (gx % 32 == 0) {
 		const uint64_t wpr = gx >> 5;
-		rpu = wpr >= 1024 ? 1 : 1024 / wpr;
+		rpu = wpr >= 32 ? 1 : 32 / wpr;
 	} else {
 		uint64_t a = gx, b = 32;
 		while (b) { uint64_t r = a % b; a = b; b = r; }
@@ -490,8 +622,9 @@ SolidUnits solid_units(const uint32_t grid[3]) {
 	SolidUnits s;
 	s.aligned = gx % 32 == 0;
 	if (s.aligned) {
+		// one 32-word window per unit when rows fit in it (32 / words-per-row rows), else one row
 		const uint64_t wpr = gx >> 5;
-		s.rows_per_unit = wpr >= 1024 ? 1 : 1024 / wpr;
+		s.rows_per_unit = wpr >= 32 ? 1 : 32 / wpr;
 	} else {
 		uint64_t a = gx, b = 32;
 		while (b) { uint64_t r = a % b; a = b; b = r; }
@@ -520,13 +653,17 @@ static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int col
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_resolve", s);
 		}
-		if (L.n_mwords) {
-			solid_morton<<<(unsigned)((L.n_mwords + 255) / 256), 256, 0, s>>>(L);
+		if (L.n_mbricks) {
+			solid_morton_brick<<<(unsigned)L.n_mbricks, 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_morton", s);
+		}
+		if (L.n_mwords) {
+			solid_morton_small<<<(unsigned)((L.n_mwords + 255) / 256), 256, 0, s>>>(L);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			solid_zero<<<(L.n_units + 7) / 8, 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
-			if (prof) (*prof)("solid_zero", s);
+			if (prof) (*prof)("solid_morton_small", s);
 		}
 	}
 	return cudaSuccess;

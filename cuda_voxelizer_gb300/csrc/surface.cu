@@ -87,9 +87,43 @@ struct WordSink {
 	}
 };
 
+// Exclusive prefix sum over the CTA (kTile threads); returns this thread's offset, total in *total.
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	uint32_t incl = v;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		const uint32_t u = __shfl_up_sync(FULL, incl, d);
+		if (lane >= (uint32_t)d) incl += u;
+	}
+	if (lane == 31) s_warp[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		uint32_t w = lane < kTile / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const uint32_t u = __shfl_up_sync(FULL, w, d);
+			if (lane >= (uint32_t)d) w += u;
+		}
+		if (lane < kTile / 32) s_warp[lane] = w;  // inclusive warp prefix
+	}
+	__syncthreads();
+	*total = s_warp[kTile / 32 - 1];
+	return (warp ? s_warp[warp - 1] : 0u) + incl - v;
+}
+
+// Phase 1: one thread per triangle (setup, classify, queue the big ones, park the small ones'
+// setup in shared memory).  Phase 2: the rows of all small triangles of the tile are dealt out
+// evenly over the CTA, one (triangle, row) item per thread at a time, so that no thread idles while
+// another walks a larger bounding box.
 template <class P>
 __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_vox) {
-	__shared__ __align__(16) float s_tri[kTile * 9];
+	__shared__ __align__(16) union {
+		float tri[kTile * 9];
+		SmallTri small[kTile];
+	} sm;
+	__shared__ uint32_t s_off[kTile + 1];
+	__shared__ uint32_t s_warp[kTile / 32];
 	__shared__ __align__(8) uint64_t s_bar;
 	const uint32_t tile = blockIdx.x;
 	const uint32_t j = job_of_tile(L, tile);
@@ -103,45 +137,31 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 	const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
 	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
 	const uint32_t cnt = (uint32_t)umin64((uint64_t)kTile, n - t0);
-	stage_tile(L, tris + t0 * 9, cnt, s_tri, &s_bar);
+	stage_tile(L, tris + t0 * 9, cnt, sm.tri, &s_bar);
 
 	const uint32_t lane = threadIdx.x & 31u;
 	const bool valid = threadIdx.x < cnt;
-	bool is_mid = false, is_big = false;
-	uint32_t n_items = 0;
-	if (valid) {
-		float t[9];
+	float t[9];
 #pragma unroll
-		for (int k = 0; k < 9; k++) t[k] = s_tri[threadIdx.x * 9 + k];
+	for (int k = 0; k < 9; k++) t[k] = valid ? sm.tri[threadIdx.x * 9 + k] : 0.0f;
+	__syncthreads();  // the tile is consumed; its shared memory now holds SmallTri records
+
+	bool is_mid = false, is_big = false;
+	uint32_t n_items = 0, n_rows = 0;
+	if (valid) {
 		SurfTri S;
 		surf_setup<P>(t, bmin, unit, grid, S);
 		const uint64_t nvox = (uint64_t)(S.bx1 - S.bx0 + 1) * (uint64_t)(S.by1 - S.by0 + 1) * (uint64_t)(S.bz1 - S.bz0 + 1);
-		if (nvox <= small_vox) {
-			// Small triangle: test every voxel of its bbox (src/voxelize.cu:136-183).
-			WordSink sink{table};
-			for (int z = S.bz0; z <= S.bz1; z++) {
-				const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
-				for (int y = S.by0; y <= S.by1; y++) {
-					const float py = __fmul_rn(__int2float_rn(y), unit[1]);
-					if (yz_fail_bits<P>(S, py, pz)) continue;
-					RowK K;
-					row_consts<P>(S, py, pz, K);
-					const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
-					const uint64_t yzm = morton ? ((spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2)) : 0;
-					for (int x = S.bx0; x <= S.bx1; x++) {
-						if (fail_bits<P>(S, K, unit[0], x)) continue;
-						sink.add(morton ? (spread3((uint32_t)x) | yzm) : base + (uint64_t)x);
-					}
-				}
-			}
-			sink.flush();
+		if (nvox <= small_vox && nvox <= 255) {
+			pack_small(S, sm.small[threadIdx.x]);
+			n_rows = (uint32_t)((S.by1 - S.by0 + 1) * (S.bz1 - S.bz0 + 1));
 		} else {
 			n_items = (uint32_t)((S.bz1 - S.bz0 + kZch) / kZch);
 			is_mid = n_items == 1;
 			is_big = n_items > 1;
 		}
 	}
-	// Queue the remaining triangles: warp-aggregated appends.
+	// Queue the other triangles: warp-aggregated appends.
 	const uint32_t lt = (1u << lane) - 1u;
 	const uint32_t mid_ballot = __ballot_sync(FULL, is_mid);
 	if (mid_ballot) {
@@ -177,6 +197,38 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 				set_error(L, kErrQueueOverflow);
 		}
 	}
+
+	// Phase 2: rows of the small triangles (src/voxelize.cu:136-183, every voxel of each row).
+	uint32_t total_rows = 0;
+	const uint32_t off = block_scan(n_rows, s_warp, &total_rows);
+	s_off[threadIdx.x] = off;
+	if (threadIdx.x == kTile - 1) s_off[kTile] = total_rows;
+	__syncthreads();
+	for (uint32_t k = threadIdx.x; k < total_rows; k += kTile) {
+		uint32_t lo = 0, hi = kTile;  // last triangle whose first row is <= k
+		while (hi - lo > 1) {
+			const uint32_t mid = (lo + hi) >> 1;
+			if (s_off[mid] <= k) lo = mid; else hi = mid;
+		}
+		SurfTri S;
+		unpack_small(sm.small[lo], S);
+		const uint32_t r = k - s_off[lo];
+		const uint32_t ny = (uint32_t)(S.by1 - S.by0 + 1);
+		const int y = S.by0 + (int)(r % ny), z = S.bz0 + (int)(r / ny);
+		const float py = __fmul_rn(__int2float_rn(y), unit[1]);
+		const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
+		if (yz_fail_bits<P>(S, py, pz)) continue;
+		RowK K;
+		row_consts<P>(S, py, pz, K);
+		WordSink sink{table};
+		const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
+		const uint64_t yzm = morton ? ((spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2)) : 0;
+		for (int x = S.bx0; x <= S.bx1; x++) {
+			if (!voxel_pass<P>(S, K, unit[0], x)) continue;
+			sink.add(morton ? (spread3((uint32_t)x) | yzm) : base + (uint64_t)x);
+		}
+		sink.flush();
+	}
 }
 
 template <class P>
@@ -188,6 +240,9 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 	const uint64_t n_big_items = bigc & kBigItemMask;
 	const uint32_t n_mid = min(*reinterpret_cast<volatile unsigned*>(&C->mid), L.scr.cap);
 	const uint64_t total = n_big_items + n_mid;
+	// Warps beyond the number of queued items have nothing to claim: they leave without touching
+	// the ticket counter (all of them do when only small triangles were queued).
+	if ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) >= total) return;
 	for (;;) {
 		unsigned long long tk = 0;
 		if (lane == 0) tk = atomicAdd(&C->ticket, 1ull);

@@ -153,6 +153,69 @@ __device__ __forceinline__ uint32_t fail_bits(const SurfTri& S, const RowK& K, f
 	return f;
 }
 
+// All x-dependent tests at once, as one pass/fail (the small-triangle path needs no more).
+template <class P>
+__device__ __forceinline__ bool voxel_pass(const SurfTri& S, const RowK& K, float ux, int x) {
+	const float px = __fmul_rn(__int2float_rn(x), ux);
+	float s;
+	if constexpr (P::plane == 1) s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.nx, px, K.kpl));
+	else if constexpr (P::plane == 2) s = __fadd_rn(__fmaf_rn(S.nx, px, K.kpl), K.kpl2);
+	else if constexpr (P::plane == 3) s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.ny, K.py, __fmul_rn(S.nx, px)));
+	else s = __fadd_rn(__fadd_rn(__fmul_rn(S.nx, px), K.kpl), K.kpl2);
+	bool ok = !(__fmul_rn(__fadd_rn(s, S.d1), __fadd_rn(s, S.d2)) > 0.0f);
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		float v;
+		if constexpr (P::edge_xy == 1) v = __fmaf_rn(S.exy[i][0], px, K.kxy[i]);
+		else v = mul_add<P::edge_xy>(S.exy[i][0], px, S.exy[i][1], K.py);
+		ok = ok && !(__fadd_rn(v, S.dxy[i]) < 0.0f);
+	}
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		float v;
+		if constexpr (P::edge_zx == 2) v = __fmaf_rn(S.ezx[i][1], px, K.kzx[i]);
+		else v = mul_add<P::edge_zx>(S.ezx[i][0], K.pz, S.ezx[i][1], px);
+		ok = ok && !(__fadd_rn(v, S.dzx[i]) < 0.0f);
+	}
+	return ok;
+}
+
+// A small triangle's setup parked in shared memory between the two phases of the classify kernel
+// (36 words): SurfTri without the bbox maxima, which are packed as extents (each below 256).
+struct SmallTri {
+	float v[32];           // nx ny nz d1 d2, exy[3][2], eyz[3][2], ezx[3][2], dxy[3], dyz[3], dzx[3]
+	int bx0, by0, bz0;
+	uint32_t ext;          // (bx1-bx0) | (by1-by0) << 8 | (bz1-bz0) << 16
+};
+
+__device__ __forceinline__ void pack_small(const SurfTri& S, SmallTri& o) {
+	o.v[0] = S.nx; o.v[1] = S.ny; o.v[2] = S.nz; o.v[3] = S.d1; o.v[4] = S.d2;
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		o.v[5 + 2 * i] = S.exy[i][0]; o.v[6 + 2 * i] = S.exy[i][1];
+		o.v[11 + 2 * i] = S.eyz[i][0]; o.v[12 + 2 * i] = S.eyz[i][1];
+		o.v[17 + 2 * i] = S.ezx[i][0]; o.v[18 + 2 * i] = S.ezx[i][1];
+		o.v[23 + i] = S.dxy[i]; o.v[26 + i] = S.dyz[i]; o.v[29 + i] = S.dzx[i];
+	}
+	o.bx0 = S.bx0; o.by0 = S.by0; o.bz0 = S.bz0;
+	o.ext = (uint32_t)(S.bx1 - S.bx0) | ((uint32_t)(S.by1 - S.by0) << 8) | ((uint32_t)(S.bz1 - S.bz0) << 16);
+}
+
+__device__ __forceinline__ void unpack_small(const SmallTri& o, SurfTri& S) {
+	S.nx = o.v[0]; S.ny = o.v[1]; S.nz = o.v[2]; S.d1 = o.v[3]; S.d2 = o.v[4];
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		S.exy[i][0] = o.v[5 + 2 * i]; S.exy[i][1] = o.v[6 + 2 * i];
+		S.eyz[i][0] = o.v[11 + 2 * i]; S.eyz[i][1] = o.v[12 + 2 * i];
+		S.ezx[i][0] = o.v[17 + 2 * i]; S.ezx[i][1] = o.v[18 + 2 * i];
+		S.dxy[i] = o.v[23 + i]; S.dyz[i] = o.v[26 + i]; S.dzx[i] = o.v[29 + i];
+	}
+	S.bx0 = o.bx0; S.by0 = o.by0; S.bz0 = o.bz0;
+	S.bx1 = o.bx0 + (int)(o.ext & 0xFFu);
+	S.by1 = o.by0 + (int)((o.ext >> 8) & 0xFFu);
+	S.bz1 = o.bz0 + (int)((o.ext >> 16) & 0xFFu);
+}
+
 // YZ edge tests for row (y, z): independent of x.  Bit i set = YZ edge i fails.
 template <class P>
 __device__ __forceinline__ uint32_t yz_fail_bits(const SurfTri& S, float py, float pz) {
