@@ -215,6 +215,8 @@ JobDesc make_job(const cvx_voxinfo& v, const float* tris, uint32_t* table, int m
 	for (int i = 0; i < 3; i++) {
 		j.bmin[i] = v.bbox_min[i];
 		j.unit[i] = v.unit[i];
+		volatile float one = 1.0f;
+		j.inv_unit[i] = one / v.unit[i];  // IEEE single division: correctly rounded
 		j.grid[i] = v.gridsize[i];
 	}
 	j.flags = (morton ? JOB_MORTON : 0u) | (solid ? JOB_SOLID : 0u);
@@ -228,13 +230,15 @@ struct Group {
 	std::vector<JobDesc> jobs;
 	uint64_t tris = 0;
 	uint32_t tiles = 0, units = 0;
-	uint64_t mwords = 0, mbricks = 0;
+	uint64_t mwords = 0, mbricks = 0, mslabs = 0;
+	uint32_t slab_smem = 0;
 };
 
 void finish_group(Group& g, bool solid) {
 	uint32_t tile = 0, unit = 0;
-	uint64_t mw = 0, mb = 0;
+	uint64_t mw = 0, mb = 0, ms = 0;
 	g.tris = 0;
+	g.slab_smem = 0;
 	for (JobDesc& j : g.jobs) {
 		j.tile_begin = tile;
 		tile += tiles_of(j.n_tri);
@@ -244,10 +248,20 @@ void finish_group(Group& g, bool solid) {
 			unit += (uint32_t)solid_units(j.grid).units;
 			j.mword_begin = mw;
 			j.mbrick_begin = mb;
+			j.mslab_begin = ms;
 			const uint64_t vox = (uint64_t)j.grid[0] * j.grid[1] * j.grid[2];
 			if (j.flags & JOB_MORTON) {
-				if (j.grid[0] >= 32) mb += vox >> 15;  // 32^3 voxels per brick
-				else mw += (vox + 31) / 32;
+				const uint64_t gx = j.grid[0];
+				if (morton_slab_grid(gx)) {
+					ms += (gx / 16) * (gx / 16);  // slabs of 16 x 16 rows
+					const uint32_t stride = (uint32_t)(gx / 32) | 1u;
+					g.slab_smem = std::max(g.slab_smem, 256u * stride * 4u);
+				} else if (gx >= 32) {
+					const uint64_t w = gx >= 128 ? 4 : gx / 32;  // x-adjacent 32^3 bricks per CTA
+					mb += (vox >> 15) / w;
+				} else {
+					mw += (vox + 31) / 32;
+				}
 			}
 		}
 	}
@@ -255,6 +269,7 @@ void finish_group(Group& g, bool solid) {
 	g.units = unit;
 	g.mwords = mw;
 	g.mbricks = mb;
+	g.mslabs = ms;
 }
 
 // Split jobs of one mode into launch groups of fewer than kMaxTriPerLaunch triangles.  A job above
@@ -321,6 +336,8 @@ struct Runner {
 		L.n_units = g.units;
 		L.n_mwords = g.mwords;
 		L.n_mbricks = g.mbricks;
+		L.n_mslabs = g.mslabs;
+		L.slab_smem = g.slab_smem;
 		L.scr.ctr = reinterpret_cast<Counters*>(rec);
 		const RecLayout lay = rec_layout(cap, 0);
 		L.scr.big = reinterpret_cast<BigRec*>(rec + lay.big);
@@ -701,6 +718,8 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 			L.n_units = g.units;
 			L.n_mwords = g.mwords;
 			L.n_mbricks = g.mbricks;
+			L.n_mslabs = g.mslabs;
+			L.slab_smem = g.slab_smem;
 			L.scr.ctr = reinterpret_cast<Counters*>(p->rec);
 			const RecLayout l0 = rec_layout(cap, 0);
 			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(p->rec) + l0.big);

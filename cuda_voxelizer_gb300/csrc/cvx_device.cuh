@@ -71,12 +71,14 @@ struct JobDesc {
 	uint64_t n_tri;
 	float bmin[3];
 	float unit[3];
+	float inv_unit[3];     // 1.0f / unit, correctly rounded (host); only used for the exactly checked div_trunc
 	uint32_t grid[3];
 	uint32_t flags;        // JOB_MORTON | JOB_SOLID
 	uint32_t tile_begin;   // first triangle tile of this job in the launch's tile space
 	uint32_t unit_begin;   // solid: first resolve unit of this job in the launch's unit space
 	uint64_t mword_begin;  // solid Morton, g < 32: first Morton word in the launch's word space
-	uint64_t mbrick_begin; // solid Morton, g >= 32: first 32^3 brick in the launch's brick space
+	uint64_t mbrick_begin; // solid Morton, g > 1024: first group of x-adjacent 32^3 bricks in the launch
+	uint64_t mslab_begin;  // solid Morton, 32 <= g <= 1024: first 16x16-row slab in the launch
 };
 
 // Work-queue records written by the classify kernels and consumed by the cooperative kernels.
@@ -118,7 +120,10 @@ struct LaunchDesc {
 	uint32_t n_tiles;      // total triangle tiles over all jobs
 	uint32_t n_units;      // solid resolve units over all jobs
 	uint64_t n_mwords;     // Morton words of solid Morton jobs with g < 32
-	uint64_t n_mbricks;    // 32^3 bricks of solid Morton jobs with g >= 32
+	uint64_t n_mbricks;    // groups of x-adjacent 32^3 bricks of solid Morton jobs with g > 1024
+	uint64_t n_mslabs;     // 16x16-row slabs of solid Morton jobs with 32 <= g <= 1024
+	uint32_t slab_smem;    // dynamic shared memory of the slab kernel (largest slab of the launch)
+	uint32_t pad2;
 	Scratch scr;
 };
 
@@ -155,6 +160,19 @@ __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) 
 }
 
 __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+// (int)__fdiv_rn(a, u) (truncation of the correctly rounded quotient, as float3_to_int3 of
+// `a / unit` in the reference, src/util.h:20-22), computed with the per-axis reciprocal inv ~ 1/u.
+// fl(a * inv) is within 2 ulp of fl(a / u); truncation can only differ when the quotient is within
+// that distance of an integer, and there the exact division decides.
+__device__ __forceinline__ int div_trunc(float a, float u, float inv) {
+	const float q = __fmul_rn(a, inv);
+	const float t = truncf(q);
+	const float room = 4.0f * __fmul_rn(fabsf(q), 1.1920929e-07f) + 1.0e-30f;  // 4 ulp-ish, never 0
+	if (fabsf(q) < 8388608.0f && q - t > room && (t + 1.0f) - q > room && fabsf(q) > room)
+		return (int)t;
+	return __float2int_rz(__fdiv_rn(a, u));
+}
 
 // Bit layout (src/voxelize.cu:50-55): word = idx / 32, bit = 31 - idx % 32 (MSB first).
 __device__ __forceinline__ uint32_t bit_of(uint64_t idx) { return 0x80000000u >> (uint32_t)(idx & 31u); }

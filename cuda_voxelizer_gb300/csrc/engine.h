@@ -11,6 +11,8 @@ constexpr uint32_t kTile = 256;        // triangles per classify CTA (one tile)
 constexpr uint32_t kZch = 32;          // z-slices per surface work item (one per lane)
 constexpr uint32_t kRowsThreads = 256; // threads per cooperative CTA
 constexpr uint32_t kColsPerItem = 256; // solid columns per work item
+constexpr uint32_t kSmallRows = 16;    // surface: rows of a triangle handled in the classify kernel
+constexpr uint32_t kSmallCols = 16;    // solid: columns of a triangle handled in the classify kernel
 
 // Device-side check codes written to Counters::error.
 enum : unsigned { kErrBulkTimeout = 1u, kErrQueueOverflow = 2u };
@@ -22,7 +24,7 @@ constexpr uint64_t kMaxTriPerLaunch = (1ull << 24) - 1;
 // Tunables (picked per device by the autotuner; defaults are safe everywhere).
 struct Tune {
 	uint32_t small_vox = 64;    // surface: bbox voxels at or below which a triangle stays in its thread
-	uint32_t small_cols = 32;   // solid: columns at or below which a triangle stays in its thread
+	uint32_t small_cols = kSmallCols;  // solid: columns at or below which a triangle stays in the classify kernel
 };
 
 // Optional per-kernel timing: mark(name) records an event on the stream after the named kernel
@@ -44,6 +46,9 @@ enum : unsigned { kSolidToggles = 1u, kSolidResolve = 2u };
 cudaError_t launch_solid(const LaunchDesc& L, const Tune& tune, int cols_grid, cudaStream_t s, unsigned phases,
                          const Prof* prof);
 int solid_cols_blocks_per_sm();
+
+// Morton grids that solid_morton_slab resolves and transcodes in one pass.
+inline bool morton_slab_grid(uint64_t g) { return g >= 32 && g <= 1024; }
 
 // Resolve-unit bookkeeping of a solid job: rows per unit and units per job.
 struct SolidUnits {

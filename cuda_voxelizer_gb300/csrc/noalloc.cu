@@ -137,6 +137,8 @@ extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const 
 	for (int i = 0; i < 3; i++) {
 		job.bmin[i] = info->bbox_min[i];
 		job.unit[i] = info->unit[i];
+		volatile float one = 1.0f;
+		job.inv_unit[i] = one / info->unit[i];
 		job.grid[i] = info->gridsize[i];
 	}
 	job.flags = (morton ? JOB_MORTON : 0u) | JOB_SOLID;
@@ -166,8 +168,14 @@ extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const 
 	L.n_tiles = 0;
 	L.n_units = (uint32_t)su.units;
 	if (morton) {
-		if (g0 >= 32) L.n_mbricks = (g0 * g1 * g2) >> 15;
-		else L.n_mwords = words;
+		if (morton_slab_grid(g0)) {
+			L.n_mslabs = (g0 / 16) * (g0 / 16);
+			L.slab_smem = 256u * ((uint32_t)(g0 / 32) | 1u) * 4u;
+		} else if (g0 >= 32) {
+			L.n_mbricks = ((g0 * g1 * g2) >> 15) / (g0 >= 128 ? 4 : g0 / 32);
+		} else {
+			L.n_mwords = words;
+		}
 	}
 	return cuda_status(launch_solid(L, tune, cols_grid, s, kSolidResolve, nullptr), "solid resolve");
 }

@@ -36,6 +36,25 @@ __device__ __forceinline__ float floor_half(float q) {
 __device__ __forceinline__ float ceil_half(float q) {
 	return fabsf(q) < 4194304.0f ? ceilf(__fsub_rn(q, 0.5f)) : (float)ceil((double)q - 0.5);
 }
+// floor_half / ceil_half of fl(a / u), using the reciprocal shortcut when the approximate
+// quotient is clearly away from the decision boundary (the half-integers), as div_trunc does.
+__device__ __forceinline__ float div_floor_half(float a, float u, float inv) {
+	const float q = __fmul_rn(a, inv);
+	const float h = __fsub_rn(q, 0.5f);
+	const float f = floorf(h);
+	const float room = 4.0f * __fmul_rn(fabsf(q), 1.1920929e-07f) + 1.0e-30f;
+	if (fabsf(q) < 4194304.0f && h - f > room && (f + 1.0f) - h > room) return f;
+	return floor_half(__fdiv_rn(a, u));
+}
+__device__ __forceinline__ float div_ceil_half(float a, float u, float inv) {
+	const float q = __fmul_rn(a, inv);
+	const float h = __fsub_rn(q, 0.5f);
+	const float f = floorf(h);
+	const float room = 4.0f * __fmul_rn(fabsf(q), 1.1920929e-07f) + 1.0e-30f;
+	if (fabsf(q) < 4194304.0f && h - f > room && (f + 1.0f) - h > room) return f + 1.0f;
+	return ceil_half(__fdiv_rn(a, u));
+}
+
 // int((double)q - 0.5) (truncation, saturating as cvt.rzi.s32.f64 does)
 __device__ __forceinline__ int trunc_half(float q) {
 	return fabsf(q) < 4194304.0f ? __float2int_rz(__fsub_rn(q, 0.5f)) : __double2int_rz((double)q - 0.5);
@@ -51,8 +70,8 @@ struct SolidTri {
 
 // Triangle setup, src/voxelize_solid.cu:83-119.
 template <class P>
-__device__ __forceinline__ void solid_setup(const float* t, const float* bmin, const float* unit, const uint32_t* grid,
-                                            SolidTri& S) {
+__device__ __forceinline__ void solid_setup(const float* t, const float* bmin, const float* unit, const float* inv,
+                                            const uint32_t* grid, SolidTri& S) {
 	const float v0x = __fsub_rn(t[0], bmin[0]), v0y = __fsub_rn(t[1], bmin[1]), v0z = __fsub_rn(t[2], bmin[2]);
 	const float v1x = __fsub_rn(t[3], bmin[0]), v1y = __fsub_rn(t[4], bmin[1]), v1z = __fsub_rn(t[5], bmin[2]);
 	const float v2x = __fsub_rn(t[6], bmin[0]), v2y = __fsub_rn(t[7], bmin[1]), v2z = __fsub_rn(t[8], bmin[2]);
@@ -61,10 +80,10 @@ __device__ __forceinline__ void solid_setup(const float* t, const float* bmin, c
 	const float cx = mul_sub<P::cross>(e0y, e1z, e0z, e1y);
 	const float cy = mul_sub<P::cross>(e0z, e1x, e0x, e1z);
 	const float cz = mul_sub<P::cross>(e0x, e1y, e0y, e1x);
-	const float inv = rsqrtf(dot3<P::dot3>(cx, cy, cz, cx, cy, cz));
-	S.nx = __fmul_rn(cx, inv);
-	S.ny = __fmul_rn(cy, inv);
-	S.nz = __fmul_rn(cz, inv);
+	const float rlen = rsqrtf(dot3<P::dot3>(cx, cy, cz, cx, cy, cz));
+	S.nx = __fmul_rn(cx, rlen);
+	S.ny = __fmul_rn(cy, rlen);
+	S.nz = __fmul_rn(cz, rlen);
 	S.v0x = v0x; S.v0y = v0y; S.v0z = v0z;
 	S.skip = fabsf(S.nx) <= kFloatErrorBelow;  // :92, (double)|n.x| < 1e-6 (the thread returns)
 	// YZ projection, made counter-clockwise (:95-105; checkCCW :55-64)
@@ -80,10 +99,10 @@ __device__ __forceinline__ void solid_setup(const float* t, const float* bmin, c
 	// table or into neighbouring rows).
 	const float mxy = fmaxf(ax, fmaxf(bx, qx)), mxz = fmaxf(ay, fmaxf(by, qy));
 	const float mny = fminf(ax, fminf(bx, qx)), mnz = fminf(ay, fminf(by, qy));
-	const float gmaxy = floor_half(__fdiv_rn(mxy, unit[1]));
-	const float gmaxz = floor_half(__fdiv_rn(mxz, unit[2]));
-	const float gminy = ceil_half(__fdiv_rn(mny, unit[1]));
-	const float gminz = ceil_half(__fdiv_rn(mnz, unit[2]));
+	const float gmaxy = div_floor_half(mxy, unit[1], inv[1]);
+	const float gmaxz = div_floor_half(mxz, unit[2], inv[2]);
+	const float gminy = div_ceil_half(mny, unit[1], inv[1]);
+	const float gminz = div_ceil_half(mnz, unit[2], inv[2]);
 	int y0 = __float2int_rz(gminy), z0 = __float2int_rz(gminz);
 	// last integer y with (float)y <= gmax (gmax holds an integer value, or is not finite)
 	int y1 = gmaxy >= 2147483520.0f ? 2147483647 : (gmaxy >= -2147483648.0f ? (int)gmaxy : (-2147483647 - 1));
@@ -235,7 +254,7 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 		float tri[kTile * 9];
 		SmallSolid small[kTile];
 	} sm;
-	__shared__ uint32_t s_off[kTile + 1];
+	__shared__ uint32_t s_items[kTile * kSmallCols];  // (triangle | dy << 8 | dz << 16) per column
 	__shared__ uint32_t s_warp[kTile / 32];
 	__shared__ __align__(8) uint64_t s_bar;
 	const uint32_t tile = blockIdx.x;
@@ -245,6 +264,7 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 	const bool morton = (J.flags & JOB_MORTON) != 0;
 	const float bmin[3] = {J.bmin[0], J.bmin[1], J.bmin[2]};
 	const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
+	const float inv[3] = {J.inv_unit[0], J.inv_unit[1], J.inv_unit[2]};
 	const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
 	uint32_t* flips = J.flips;
 	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
@@ -262,10 +282,10 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 	uint32_t n_items = 0, n_cols = 0;
 	if (valid) {
 		SolidTri S;
-		solid_setup<P>(t, bmin, unit, grid, S);
+		solid_setup<P>(t, bmin, unit, inv, grid, S);
 		if (!S.skip && S.y0 <= S.y1 && S.z0 <= S.z1) {
 			const uint64_t ncols = (uint64_t)(S.y1 - S.y0 + 1) * (uint64_t)(S.z1 - S.z0 + 1);
-			if (ncols <= small_cols && S.y1 - S.y0 < 65536 && S.z1 - S.z0 < 65536) {
+			if (ncols <= small_cols && ncols <= kSmallCols) {
 				SmallSolid& o = sm.small[threadIdx.x];
 				o.nx = S.nx; o.ny = S.ny; o.nz = S.nz; o.v0x = S.v0x; o.v0y = S.v0y; o.v0z = S.v0z;
 				o.ax = S.ax; o.ay = S.ay; o.bx = S.bx; o.by = S.by; o.cx = S.cx; o.cy = S.cy;
@@ -319,22 +339,19 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 	// Phase 2: columns of the small triangles (src/voxelize_solid.cu:115-139).
 	uint32_t total_cols = 0;
 	const uint32_t off = block_scan(n_cols, s_warp, &total_cols);
-	s_off[threadIdx.x] = off;
-	if (threadIdx.x == kTile - 1) s_off[kTile] = total_cols;
+	if (n_cols) {
+		const uint32_t nzc = (sm.small[threadIdx.x].ext >> 16) + 1u;
+		for (uint32_t c = 0; c < n_cols; c++)
+			s_items[off + c] = threadIdx.x | ((c / nzc) << 8) | ((c % nzc) << 16);
+	}
 	__syncthreads();
 	for (uint32_t k = threadIdx.x; k < total_cols; k += kTile) {
-		uint32_t lo = 0, hi = kTile;
-		while (hi - lo > 1) {
-			const uint32_t mid = (lo + hi) >> 1;
-			if (s_off[mid] <= k) lo = mid; else hi = mid;
-		}
-		const SmallSolid& o = sm.small[lo];
+		const uint32_t it = s_items[k];
+		const SmallSolid& o = sm.small[it & 0xFFu];
 		SolidTri S;
 		S.nx = o.nx; S.ny = o.ny; S.nz = o.nz; S.v0x = o.v0x; S.v0y = o.v0y; S.v0z = o.v0z;
 		S.ax = o.ax; S.ay = o.ay; S.bx = o.bx; S.by = o.by; S.cx = o.cx; S.cy = o.cy;
-		const uint32_t c = k - s_off[lo];
-		const uint32_t nzc = (o.ext >> 16) + 1u;
-		const int y = o.y0 + (int)(c / nzc), z = o.z0 + (int)(c % nzc);
+		const int y = o.y0 + (int)((it >> 8) & 0xFFu), z = o.z0 + (int)(it >> 16);
 		int xmax;
 		if (column_hit<P>(S, unit, y, z, xmax)) record_hit(flips, grid, morton, y, z, xmax);
 	}
@@ -344,10 +361,17 @@ template <class P>
 __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant__ LaunchDesc L) {
 	const uint32_t lane = threadIdx.x & 31u;
 	Counters* C = L.scr.ctr;
-	const unsigned long long bigc = *reinterpret_cast<volatile unsigned long long*>(&C->big);
+	__shared__ unsigned long long s_bigc;  // read once per CTA (see surf_rows)
+	__shared__ unsigned s_mid;
+	if (threadIdx.x == 0) {
+		s_bigc = *reinterpret_cast<volatile unsigned long long*>(&C->big);
+		s_mid = *reinterpret_cast<volatile unsigned*>(&C->mid);
+	}
+	__syncthreads();
+	const unsigned long long bigc = s_bigc;
 	const uint32_t n_big = min((uint32_t)(bigc >> kBigShift), L.scr.cap);
 	const uint64_t n_big_items = bigc & kBigItemMask;
-	const uint32_t n_mid = min(*reinterpret_cast<volatile unsigned*>(&C->mid), L.scr.cap);
+	const uint32_t n_mid = min(s_mid, L.scr.cap);
 	const uint64_t total = n_big_items + n_mid;
 	// Warps beyond the number of queued items have nothing to claim: they leave without touching
 	// the ticket counter (all of them do when only small triangles were queued).
@@ -392,7 +416,7 @@ __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant
 #pragma unroll
 		for (int k = 0; k < 9; k++) t[k] = __shfl_sync(FULL, tv, k);
 		SolidTri S;
-		solid_setup<P>(t, J.bmin, unit, grid, S);
+		solid_setup<P>(t, J.bmin, unit, J.inv_unit, grid, S);
 		const uint64_t nzc = (uint64_t)(S.z1 - S.z0 + 1);
 		const uint64_t ncols = (uint64_t)(S.y1 - S.y0 + 1) * nzc;
 		const uint64_t c0 = (uint64_t)chunk * kColsPerItem;
@@ -421,10 +445,33 @@ __device__ __forceinline__ uint32_t prefix_xor_msb(uint32_t t) {
 	return t;
 }
 
-// One warp per resolve unit.  A unit is a run of whole rows starting on a word boundary.
+// Morton grids resolved and transcoded in one pass by solid_morton_slab (cubic powers of two).
+__host__ __device__ __forceinline__ bool slab_grid(uint64_t g) { return g >= 32 && g <= 1024; }
+
+// Resolve one word: toggles t (MSB first) plus the parity carried in from the row's earlier words.
+__device__ __forceinline__ uint32_t resolve_word(uint32_t t, uint32_t& carry) {
+	const uint32_t res = prefix_xor_msb(t) ^ (carry ? 0xFFFFFFFFu : 0u);
+	carry = res & 1u;  // the row's parity after this word's last bit
+	return res;
+}
+
+// Linear jobs: table ^= resolved, toggles cleared.  Morton jobs: toggles replaced by the resolved
+// bits for solid_morton_* to gather.
+__device__ __forceinline__ void resolve_store(uint32_t* flips, uint32_t* dest, uint64_t w, uint32_t t, uint32_t res,
+                                              bool morton) {
+	if (morton) {
+		if (res != t) flips[w] = res;
+	} else {
+		if (res) dest[w] ^= res;
+		if (t) flips[w] = 0u;
+	}
+}
+
+// One thread per resolve unit.  gx a multiple of 32: a unit is one row (whole words; 16-byte
+// loads when the row and both tables are 16-byte aligned).  Other gx: the shortest run of rows
+// that starts and ends on word boundaries, walked bit by bit (odd grid sizes only).
 __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ LaunchDesc L) {
-	const uint32_t lane = threadIdx.x & 31u;
-	const uint32_t unit_id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	const uint32_t unit_id = blockIdx.x * blockDim.x + threadIdx.x;
 	if (unit_id >= L.n_units) return;
 	const uint32_t j = job_search(L, unit_id, [](const JobDesc& d) { return (uint64_t)d.unit_begin; });
 	const JobDesc& J = job_at(L, j);
@@ -434,53 +481,39 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 	uint32_t* flips = J.flips;
 	uint32_t* dest = J.table;
 	const uint64_t u = unit_id - J.unit_begin;
+	if (morton && slab_grid(gx)) return;  // solid_morton_slab resolves these jobs itself
 	if (gx % 32 == 0) {
-		// 32-bit arithmetic only (64-bit division is a slow software routine): gx <= 2^22, so a
-		// row has at most 2^17 words.  A unit is one 32-word window when rows fit in it.
 		const uint32_t wpr = (uint32_t)(gx >> 5);
-		const uint32_t rpu = wpr >= 32 ? 1u : 32u / wpr;
-		const uint64_t r0 = u * rpu, r1 = umin64(rows, r0 + rpu);
-		const uint64_t wbeg = r0 * wpr, wend = r1 * wpr;
-		const bool pow2 = (wpr & (wpr - 1)) == 0;
+		const uint64_t w0 = u * wpr;
 		uint32_t carry = 0;
-		for (uint64_t wb = wbeg; wb < wend; wb += 32) {
-			const uint64_t w = wb + lane;
-			const bool active = w < wend;
-			const uint32_t t = active ? flips[w] : 0u;
-			const uint32_t x = __popc(t) & 1u;
-			const uint32_t off = (uint32_t)(wb - wbeg) + lane;
-			uint32_t v = x;
-			bool f = active && (pow2 ? (off & (wpr - 1)) == 0 : off % wpr == 0);
-#pragma unroll
-			for (int d = 1; d < 32; d <<= 1) {
-				const uint32_t uv = __shfl_up_sync(FULL, v, d);
-				const bool uf = __shfl_up_sync(FULL, (int)f, d) != 0;
-				if (lane >= (uint32_t)d) {
-					if (!f) v ^= uv;
-					f = f || uf;
-				}
-			}
-			const uint32_t vin = f ? v : (v ^ carry);
-			const uint32_t res = prefix_xor_msb(t) ^ ((vin ^ x) ? 0xFFFFFFFFu : 0u);
-			if (active) {
+		const bool vec = (wpr & 3u) == 0 && ((reinterpret_cast<uintptr_t>(flips + w0) | reinterpret_cast<uintptr_t>(dest + w0)) & 15u) == 0;
+		if (vec) {
+			for (uint32_t i = 0; i < wpr; i += 4) {
+				const uint4 t = *reinterpret_cast<const uint4*>(flips + w0 + i);
+				if ((t.x | t.y | t.z | t.w) == 0u && carry == 0u) continue;  // outside the solid
+				const uint32_t r0 = resolve_word(t.x, carry), r1 = resolve_word(t.y, carry);
+				const uint32_t r2 = resolve_word(t.z, carry), r3 = resolve_word(t.w, carry);
 				if (morton) {
-					flips[w] = res;
+					*reinterpret_cast<uint4*>(flips + w0 + i) = make_uint4(r0, r1, r2, r3);
 				} else {
-					if (res) dest[w] ^= res;
-					if (t) flips[w] = 0u;
+					uint4 d = *reinterpret_cast<const uint4*>(dest + w0 + i);
+					d.x ^= r0; d.y ^= r1; d.z ^= r2; d.w ^= r3;
+					*reinterpret_cast<uint4*>(dest + w0 + i) = d;
+					if (t.x | t.y | t.z | t.w) *reinterpret_cast<uint4*>(flips + w0 + i) = make_uint4(0u, 0u, 0u, 0u);
 				}
 			}
-			carry = __shfl_sync(FULL, vin, 31);
+		} else {
+			for (uint32_t i = 0; i < wpr; i++) {
+				const uint32_t t = flips[w0 + i];
+				if (t == 0u && carry == 0u) continue;
+				resolve_store(flips, dest, w0 + i, t, resolve_word(t, carry), morton);
+			}
 		}
-	} else if (lane == 0) {
-		// Rows not word aligned: walk the unit's bits serially (odd grid sizes only).
+	} else {
 		const uint64_t g = gx;
-		uint64_t p = 32;  // lcm(gx, 32) / gx rows per unit
-		{
-			uint64_t a = g, b = 32;
-			while (b) { uint64_t r = a % b; a = b; b = r; }
-			p = 32 / a;
-		}
+		uint64_t a = g, bb = 32;
+		while (bb) { const uint64_t r = a % bb; a = bb; bb = r; }
+		const uint64_t p = 32 / a;  // rows per unit: lcm(gx, 32) / gx
 		const uint64_t r0 = u * p, r1 = umin64(rows, r0 + p);
 		const uint64_t b0 = r0 * g, b1 = r1 * g;
 		uint32_t carry = 0;
@@ -489,21 +522,16 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 			const uint32_t t = flips[w];
 			uint32_t res = 0;
 			for (uint32_t k = 0; k < 32; k++) {
-				const uint64_t b = (w << 5) + k;
-				if (b >= b1) break;
-				if (b == next_row) {
+				const uint64_t bit = (w << 5) + k;
+				if (bit >= b1) break;
+				if (bit == next_row) {
 					carry = 0;
 					next_row += g;
 				}
 				carry ^= (t >> (31 - k)) & 1u;
 				res |= carry << (31 - k);
 			}
-			if (morton) {
-				flips[w] = res;
-			} else {
-				if (res) dest[w] ^= res;
-				if (t) flips[w] = 0u;
-			}
+			resolve_store(flips, dest, w, t, res, morton);
 		}
 	}
 }
@@ -530,41 +558,125 @@ __device__ __forceinline__ uint32_t nibble_mask(uint32_t nib) {
 	return m;
 }
 
-// Morton jobs with g >= 32: one CTA per Morton-aligned 32^3 brick (1,024 consecutive Morton words).
-// The brick's 32 x 32 resolved row words (32 x-bits each) are staged in shared memory and cleared
-// in the flip table (this CTA is their only reader), then each Morton word is assembled from
-// eight 4-bit row nibbles and XORed into the table with coalesced accesses.
+// Morton jobs with g >= 32: one CTA per group of W = min(4, g/32) x-adjacent Morton-aligned 32^3
+// bricks.  Each brick is 1,024 consecutive Morton words; the group's 32 x 32 rows of W*32 x-bits are
+// staged in shared memory (16-byte accesses when W = 4) and cleared in the flip table (this CTA is
+// their only reader), then each Morton word is assembled from eight 4-bit row nibbles and XORed into
+// the table with coalesced accesses.
 __global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant__ LaunchDesc L) {
-	__shared__ uint32_t s_rows[32 * 32];  // [z][y] word of x-bits of the brick
-	const uint64_t brick = blockIdx.x;
-	const uint32_t j = job_search(L, brick, [](const JobDesc& d) { return d.mbrick_begin; });
+	__shared__ __align__(16) uint32_t s_rows[32 * 32 * 4];  // [z][y][W] words of x-bits
+	const uint64_t group = blockIdx.x;
+	const uint32_t j = job_search(L, group, [](const JobDesc& d) { return d.mbrick_begin; });
 	const JobDesc& J = job_at(L, j);
 	const uint64_t g = J.grid[0];
-	const uint64_t b = brick - J.mbrick_begin;             // brick index within the job
-	const uint64_t bx = compact3(b), by = compact3(b >> 1), bz = compact3(b >> 2);
+	const uint32_t W = g >= 128 ? 4u : (uint32_t)(g >> 5);       // bricks per group
+	const uint64_t gi = group - J.mbrick_begin;                  // group index within the job
+	// groups are numbered x-fastest over (g/32/W) x (g/32) x (g/32); group gi covers the bricks
+	// (W*Bx + k, by, bz), k < W (g is a power of two: the divisions are shifts)
+	const uint32_t lg_nb = 31u - __clz((uint32_t)(g >> 5));      // log2(bricks per axis)
+	const uint32_t lg_w = W == 4 ? 2u : (W == 2 ? 1u : 0u);
+	const uint64_t Bx = gi & ((1ull << (lg_nb - lg_w)) - 1ull);
+	const uint64_t by = (gi >> (lg_nb - lg_w)) & ((1ull << lg_nb) - 1ull);
+	const uint64_t bz = gi >> (2 * lg_nb - lg_w);
+	const uint64_t bx = Bx * W;
 	uint32_t* flips = J.flips;
+	const uint64_t wpr = g >> 5;
 	for (uint32_t i = threadIdx.x; i < 1024; i += 256) {
 		const uint64_t z = bz * 32 + (i >> 5), y = by * 32 + (i & 31);
-		const uint64_t w = ((z * g + y) * g + bx * 32) >> 5;
-		const uint32_t v = flips[w];
-		s_rows[i] = v;
-		if (v) flips[w] = 0u;
+		const uint64_t w = (z * g + y) * wpr + bx;
+		if (W == 4 && ((reinterpret_cast<uintptr_t>(flips + w) & 15u) == 0)) {
+			const uint4 v = *reinterpret_cast<const uint4*>(flips + w);
+			*reinterpret_cast<uint4*>(s_rows + i * 4) = v;
+			if (v.x | v.y | v.z | v.w) *reinterpret_cast<uint4*>(flips + w) = make_uint4(0u, 0u, 0u, 0u);
+		} else {
+			for (uint32_t k = 0; k < W; k++) {
+				const uint32_t v = flips[w + k];
+				s_rows[i * 4 + k] = v;
+				if (v) flips[w + k] = 0u;
+			}
+		}
 	}
 	__syncthreads();
-	uint32_t* dest = J.table + (b << 10);
-	for (uint32_t m = threadIdx.x; m < 1024; m += 256) {
-		// local Morton word m covers x' = 4X.., y' = 4Y.., z' = 2Z.. of the brick
-		const uint32_t X = compact3(m >> 1), Y = compact3(m >> 2), Z = compact3(m);
+	for (uint32_t xk = 0; xk < W; xk++) {
+		// brick (bx + xk, by, bz): its Morton words are the 1,024 starting at its Morton index * 1024
+		const uint64_t brick = spread3((uint32_t)(bx + xk)) | (spread3((uint32_t)by) << 1) | (spread3((uint32_t)bz) << 2);
+		uint32_t* dest = J.table + (brick << 10);
+		for (uint32_t m = threadIdx.x; m < 1024; m += 256) {
+			const uint32_t X = compact3(m >> 1), Y = compact3(m >> 2), Z = compact3(m);
+			uint32_t out = 0;
+#pragma unroll
+			for (uint32_t dz = 0; dz < 2; dz++)
+#pragma unroll
+				for (uint32_t dy = 0; dy < 4; dy++) {
+					const uint32_t row = s_rows[((2 * Z + dz) * 32 + 4 * Y + dy) * 4 + xk];
+					const uint32_t nib = (row >> (28u - 4u * X)) & 0xFu;
+					out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
+				}
+			if (out) dest[m] ^= out;
+		}
+	}
+}
+
+// Morton jobs with 32 <= g <= 1024: resolve, transcode and clear in one pass.  One CTA per slab of
+// 16 x 16 rows (y block by, z block bz, 16 each): for each of its 16 z-slices the slab's 16 rows are
+// contiguous in the flip table, so they are loaded with coalesced 16-byte accesses into shared
+// memory (rows padded to an odd word count: no bank conflicts below) and cleared; each thread
+// resolves one whole row (prefix XOR along x); then every 16^3 block along x -- 128 consecutive
+// Morton words -- is gathered from 4-bit row nibbles and XORed into the table.
+__global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__ LaunchDesc L) {
+	extern __shared__ __align__(16) uint32_t s_slab[];  // [row = zi*16 + yi][stride]
+	const uint64_t slab = blockIdx.x;
+	const uint32_t j = job_search(L, slab, [](const JobDesc& d) { return d.mslab_begin; });
+	const JobDesc& J = job_at(L, j);
+	const uint64_t g = J.grid[0];
+	const uint32_t wpr = (uint32_t)(g >> 5);           // words per row
+	const uint32_t stride = wpr | 1u;
+	const uint32_t lgw = 31u - __clz(wpr);
+	const uint32_t nb = (uint32_t)(g >> 4);            // 16-blocks per axis
+	const uint32_t lgb = 31u - __clz(nb);
+	const uint64_t si = slab - J.mslab_begin;
+	const uint64_t by = si & (nb - 1u), bz = si >> lgb;
+	uint32_t* flips = J.flips;
+	const uint32_t chunk = 16u * wpr;                   // words of the slab in one z-slice
+	for (uint32_t i = threadIdx.x; i < 16u * (chunk / 4u); i += 256) {
+		const uint32_t zi = i / (chunk / 4u), q = i % (chunk / 4u);
+		uint4* src = reinterpret_cast<uint4*>(flips + ((bz * 16 + zi) * g + by * 16) * wpr) + q;
+		const uint4 v = *src;
+		const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			const uint32_t idx = 4 * q + k;
+			s_slab[(zi * 16 + (idx >> lgw)) * stride + (idx & (wpr - 1u))] = vv[k];
+		}
+		if (v.x | v.y | v.z | v.w) *src = make_uint4(0u, 0u, 0u, 0u);
+	}
+	__syncthreads();
+	{
+		uint32_t* row = s_slab + threadIdx.x * stride;  // 256 rows, one per thread
+		uint32_t carry = 0;
+		for (uint32_t w = 0; w < wpr; w++) {
+			const uint32_t t = row[w];
+			if (t == 0u && carry == 0u) continue;
+			row[w] = resolve_word(t, carry);
+		}
+	}
+	__syncthreads();
+	// 16^3 blocks along x: two per pass (128 Morton words each, one per thread)
+	const uint32_t half = threadIdx.x >> 7, m = threadIdx.x & 127u;
+	const uint32_t X = compact3(m >> 1), Y = compact3(m >> 2), Z = compact3(m);  // 2, 2, 3 bits
+	for (uint32_t bx = half; bx < nb; bx += 2) {
+		const uint64_t blk = spread3(bx) | (spread3((uint32_t)by) << 1) | (spread3((uint32_t)bz) << 2);
+		const uint32_t wsel = bx >> 1, xoff = (bx & 1u) * 16u + 4u * X;  // word, first x bit in it
 		uint32_t out = 0;
 #pragma unroll
 		for (uint32_t dz = 0; dz < 2; dz++)
 #pragma unroll
 			for (uint32_t dy = 0; dy < 4; dy++) {
-				const uint32_t row = s_rows[(2 * Z + dz) * 32 + 4 * Y + dy];
-				const uint32_t nib = (row >> (28u - 4u * X)) & 0xFu;
+				const uint32_t rw = s_slab[((2 * Z + dz) * 16 + 4 * Y + dy) * stride + wsel];
+				const uint32_t nib = (rw >> (28u - xoff)) & 0xFu;
 				out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 			}
-		if (out) dest[m] ^= out;
+		if (out) J.table[(blk << 7) + m] ^= out;
 	}
 }
 
@@ -589,29 +701,22 @@ __global__ void __launch_bounds__(256) solid_morton_small(const __grid_constant_
 	if (out) J.table[m] ^= out;
 }
 
-// Morton jobs: clear the resolved flip table, one warp per resolve unit.
+// Morton jobs with g < 32: clear the resolved flip table, one thread per resolve unit (the larger
+// grids' bricks clear their own words).
 __global__ void __launch_bounds__(256) solid_zero(const __grid_constant__ LaunchDesc L) {
-	const uint32_t lane = threadIdx.x & 31u;
-	const uint32_t unit_id = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	const uint32_t unit_id = blockIdx.x * blockDim.x + threadIdx.x;
 	if (unit_id >= L.n_units) return;
 	const uint32_t j = job_search(L, unit_id, [](const JobDesc& d) { return (uint64_t)d.unit_begin; });
 	const JobDesc& J = job_at(L, j);
-	if (!(J.flags & JOB_MORTON) || J.grid[0] >= 32) return;  // bricks clear their own words
+	if (!(J.flags & JOB_MORTON) || J.grid[0] >= 32) return;
 	const uint64_t gx = J.grid[0];
 	const uint64_t rows = (uint64_t)J.grid[1] * J.grid[2];
-	uint64_t rpu;
-	if (gx % 32 == 0) {
-		const uint64_t wpr = gx >> 5;
-		rpu = wpr >= 32 ? 1 : 32 / wpr;
-	} else {
-		uint64_t a = gx, b = 32;
-		while (b) { uint64_t r = a % b; a = b; b = r; }
-		rpu = 32 / a;
-	}
+	uint64_t a = gx, bb = 32;
+	while (bb) { const uint64_t r = a % bb; a = bb; bb = r; }
+	const uint64_t p = (gx % 32 == 0) ? 1 : 32 / a;
 	const uint64_t u = unit_id - J.unit_begin;
-	const uint64_t r0 = u * rpu, r1 = min(rows, r0 + rpu);
-	const uint64_t wbeg = (r0 * gx) >> 5, wend = (r1 * gx + 31) >> 5;
-	for (uint64_t w = wbeg + lane; w < wend; w += 32) J.flips[w] = 0u;
+	const uint64_t r0 = u * p, r1 = umin64(rows, r0 + p);
+	for (uint64_t w = (r0 * gx) >> 5; w < ((r1 * gx + 31) >> 5); w++) J.flips[w] = 0u;
 }
 
 }  // namespace
@@ -622,9 +727,7 @@ SolidUnits solid_units(const uint32_t grid[3]) {
 	SolidUnits s;
 	s.aligned = gx % 32 == 0;
 	if (s.aligned) {
-		// one 32-word window per unit when rows fit in it (32 / words-per-row rows), else one row
-		const uint64_t wpr = gx >> 5;
-		s.rows_per_unit = wpr >= 32 ? 1 : 32 / wpr;
+		s.rows_per_unit = 1;  // one row per resolve thread
 	} else {
 		uint64_t a = gx, b = 32;
 		while (b) { uint64_t r = a % b; a = b; b = r; }
@@ -649,9 +752,23 @@ static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int col
 	}
 	if (phases & kSolidResolve) {
 		if (L.n_units) {
-			solid_resolve<<<(L.n_units + 7) / 8, 256, 0, s>>>(L);
+			solid_resolve<<<(L.n_units + 255) / 256, 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_resolve", s);
+		}
+		if (L.n_mslabs) {
+			static int attr_set[64] = {};
+			int dev = 0;
+			cudaGetDevice(&dev);
+			if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+				if ((e = cudaFuncSetAttribute(solid_morton_slab, cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                              256 * (32 + 1) * 4)) != cudaSuccess)
+					return e;
+				attr_set[dev] = 1;
+			}
+			solid_morton_slab<<<(unsigned)L.n_mslabs, 256, L.slab_smem, s>>>(L);
+			if ((e = cudaGetLastError()) != cudaSuccess) return e;
+			if (prof) (*prof)("solid_morton_slab", s);
 		}
 		if (L.n_mbricks) {
 			solid_morton_brick<<<(unsigned)L.n_mbricks, 256, 0, s>>>(L);
@@ -661,7 +778,7 @@ static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int col
 		if (L.n_mwords) {
 			solid_morton_small<<<(unsigned)((L.n_mwords + 255) / 256), 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
-			solid_zero<<<(L.n_units + 7) / 8, 256, 0, s>>>(L);
+			solid_zero<<<(L.n_units + 255) / 256, 256, 0, s>>>(L);
 			if ((e = cudaGetLastError()) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_morton_small", s);
 		}

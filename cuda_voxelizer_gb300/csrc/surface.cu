@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 		float tri[kTile * 9];
 		SmallTri small[kTile];
 	} sm;
-	__shared__ uint32_t s_off[kTile + 1];
+	__shared__ uint16_t s_items[kTile * kSmallRows];  // (triangle | dy << 8 | dz << 12) per row
 	__shared__ uint32_t s_warp[kTile / 32];
 	__shared__ __align__(8) uint64_t s_bar;
 	const uint32_t tile = blockIdx.x;
@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 	const bool morton = (J.flags & JOB_MORTON) != 0;
 	const float bmin[3] = {J.bmin[0], J.bmin[1], J.bmin[2]};
 	const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
+	const float inv[3] = {J.inv_unit[0], J.inv_unit[1], J.inv_unit[2]};
 	const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
 	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
 	const uint32_t cnt = (uint32_t)umin64((uint64_t)kTile, n - t0);
@@ -150,11 +151,12 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 	uint32_t n_items = 0, n_rows = 0;
 	if (valid) {
 		SurfTri S;
-		surf_setup<P>(t, bmin, unit, grid, S);
-		const uint64_t nvox = (uint64_t)(S.bx1 - S.bx0 + 1) * (uint64_t)(S.by1 - S.by0 + 1) * (uint64_t)(S.bz1 - S.bz0 + 1);
-		if (nvox <= small_vox && nvox <= 255) {
+		surf_setup<P>(t, bmin, unit, inv, grid, S);
+		const uint64_t rows = (uint64_t)(S.by1 - S.by0 + 1) * (uint64_t)(S.bz1 - S.bz0 + 1);
+		const uint64_t nvox = (uint64_t)(S.bx1 - S.bx0 + 1) * rows;
+		if (nvox <= small_vox && nvox <= 255 && rows <= kSmallRows && S.by1 - S.by0 < 16 && S.bz1 - S.bz0 < 16) {
 			pack_small(S, sm.small[threadIdx.x]);
-			n_rows = (uint32_t)((S.by1 - S.by0 + 1) * (S.bz1 - S.bz0 + 1));
+			n_rows = (uint32_t)rows;
 		} else {
 			n_items = (uint32_t)((S.bz1 - S.bz0 + kZch) / kZch);
 			is_mid = n_items == 1;
@@ -201,20 +203,18 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 	// Phase 2: rows of the small triangles (src/voxelize.cu:136-183, every voxel of each row).
 	uint32_t total_rows = 0;
 	const uint32_t off = block_scan(n_rows, s_warp, &total_rows);
-	s_off[threadIdx.x] = off;
-	if (threadIdx.x == kTile - 1) s_off[kTile] = total_rows;
+	if (n_rows) {
+		const SmallTri& o = sm.small[threadIdx.x];
+		const uint32_t ny = ((o.ext >> 8) & 0xFFu) + 1u;
+		for (uint32_t r = 0; r < n_rows; r++)
+			s_items[off + r] = (uint16_t)(threadIdx.x | ((r % ny) << 8) | ((r / ny) << 12));
+	}
 	__syncthreads();
 	for (uint32_t k = threadIdx.x; k < total_rows; k += kTile) {
-		uint32_t lo = 0, hi = kTile;  // last triangle whose first row is <= k
-		while (hi - lo > 1) {
-			const uint32_t mid = (lo + hi) >> 1;
-			if (s_off[mid] <= k) lo = mid; else hi = mid;
-		}
+		const uint32_t it = s_items[k];
 		SurfTri S;
-		unpack_small(sm.small[lo], S);
-		const uint32_t r = k - s_off[lo];
-		const uint32_t ny = (uint32_t)(S.by1 - S.by0 + 1);
-		const int y = S.by0 + (int)(r % ny), z = S.bz0 + (int)(r / ny);
+		unpack_small(sm.small[it & 0xFFu], S);
+		const int y = S.by0 + (int)((it >> 8) & 0xFu), z = S.bz0 + (int)(it >> 12);
 		const float py = __fmul_rn(__int2float_rn(y), unit[1]);
 		const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
 		if (yz_fail_bits<P>(S, py, pz)) continue;
@@ -235,10 +235,19 @@ template <class P>
 __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant__ LaunchDesc L) {
 	const uint32_t lane = threadIdx.x & 31u;
 	Counters* C = L.scr.ctr;
-	const unsigned long long bigc = *reinterpret_cast<volatile unsigned long long*>(&C->big);
+	// One thread per CTA reads the queue counters (thousands of warps reading one line would
+	// serialise on its L2 slice), the CTA shares them through shared memory.
+	__shared__ unsigned long long s_bigc;
+	__shared__ unsigned s_mid;
+	if (threadIdx.x == 0) {
+		s_bigc = *reinterpret_cast<volatile unsigned long long*>(&C->big);
+		s_mid = *reinterpret_cast<volatile unsigned*>(&C->mid);
+	}
+	__syncthreads();
+	const unsigned long long bigc = s_bigc;
 	const uint32_t n_big = min((uint32_t)(bigc >> kBigShift), L.scr.cap);
 	const uint64_t n_big_items = bigc & kBigItemMask;
-	const uint32_t n_mid = min(*reinterpret_cast<volatile unsigned*>(&C->mid), L.scr.cap);
+	const uint32_t n_mid = min(s_mid, L.scr.cap);
 	const uint64_t total = n_big_items + n_mid;
 	// Warps beyond the number of queued items have nothing to claim: they leave without touching
 	// the ticket counter (all of them do when only small triangles were queued).
@@ -284,7 +293,7 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 #pragma unroll
 		for (int k = 0; k < 9; k++) t[k] = __shfl_sync(FULL, tv, k);
 		SurfTri S;
-		surf_setup<P>(t, J.bmin, unit, grid, S);
+		surf_setup<P>(t, J.bmin, unit, J.inv_unit, grid, S);
 		RowDirs D;
 		row_dirs(S, unit[0], D);
 

@@ -37,8 +37,8 @@ __device__ __forceinline__ float setup_dot(float ax, float vx, float ay, float v
 
 // Triangle setup, src/voxelize.cu:71-133.  `t` holds v0.xyz, v1.xyz, v2.xyz in world space.
 template <class P>
-__device__ __forceinline__ void surf_setup(const float* t, const float* bmin, const float* unit, const uint32_t* grid,
-                                           SurfTri& S) {
+__device__ __forceinline__ void surf_setup(const float* t, const float* bmin, const float* unit, const float* inv,
+                                           const uint32_t* grid, SurfTri& S) {
 	const float v0x = __fsub_rn(t[0], bmin[0]), v0y = __fsub_rn(t[1], bmin[1]), v0z = __fsub_rn(t[2], bmin[2]);
 	const float v1x = __fsub_rn(t[3], bmin[0]), v1y = __fsub_rn(t[4], bmin[1]), v1z = __fsub_rn(t[5], bmin[2]);
 	const float v2x = __fsub_rn(t[6], bmin[0]), v2y = __fsub_rn(t[7], bmin[1]), v2z = __fsub_rn(t[8], bmin[2]);
@@ -49,19 +49,19 @@ __device__ __forceinline__ void surf_setup(const float* t, const float* bmin, co
 	const float cx = mul_sub<P::cross>(e0y, e1z, e0z, e1y);
 	const float cy = mul_sub<P::cross>(e0z, e1x, e0x, e1z);
 	const float cz = mul_sub<P::cross>(e0x, e1y, e0y, e1x);
-	const float inv = rsqrtf(dot3<P::dot3>(cx, cy, cz, cx, cy, cz));
-	S.nx = __fmul_rn(cx, inv);
-	S.ny = __fmul_rn(cy, inv);
-	S.nz = __fmul_rn(cz, inv);
+	const float rlen = rsqrtf(dot3<P::dot3>(cx, cy, cz, cx, cy, cz));
+	S.nx = __fmul_rn(cx, rlen);
+	S.ny = __fmul_rn(cy, rlen);
+	S.nz = __fmul_rn(cz, rlen);
 
 	// grid bbox: clamp(int(min(v) / unit), 0, g - 1)  (:83-87)
 	const int gmx = (int)grid[0] - 1, gmy = (int)grid[1] - 1, gmz = (int)grid[2] - 1;
-	S.bx0 = min(max(__float2int_rz(__fdiv_rn(fminf(v0x, fminf(v1x, v2x)), unit[0])), 0), gmx);
-	S.by0 = min(max(__float2int_rz(__fdiv_rn(fminf(v0y, fminf(v1y, v2y)), unit[1])), 0), gmy);
-	S.bz0 = min(max(__float2int_rz(__fdiv_rn(fminf(v0z, fminf(v1z, v2z)), unit[2])), 0), gmz);
-	S.bx1 = min(max(__float2int_rz(__fdiv_rn(fmaxf(v0x, fmaxf(v1x, v2x)), unit[0])), 0), gmx);
-	S.by1 = min(max(__float2int_rz(__fdiv_rn(fmaxf(v0y, fmaxf(v1y, v2y)), unit[1])), 0), gmy);
-	S.bz1 = min(max(__float2int_rz(__fdiv_rn(fmaxf(v0z, fmaxf(v1z, v2z)), unit[2])), 0), gmz);
+	S.bx0 = min(max(div_trunc(fminf(v0x, fminf(v1x, v2x)), unit[0], inv[0]), 0), gmx);
+	S.by0 = min(max(div_trunc(fminf(v0y, fminf(v1y, v2y)), unit[1], inv[1]), 0), gmy);
+	S.bz0 = min(max(div_trunc(fminf(v0z, fminf(v1z, v2z)), unit[2], inv[2]), 0), gmz);
+	S.bx1 = min(max(div_trunc(fmaxf(v0x, fmaxf(v1x, v2x)), unit[0], inv[0]), 0), gmx);
+	S.by1 = min(max(div_trunc(fmaxf(v0y, fmaxf(v1y, v2y)), unit[1], inv[1]), 0), gmy);
+	S.bz1 = min(max(div_trunc(fmaxf(v0z, fmaxf(v1z, v2z)), unit[2], inv[2]), 0), gmz);
 
 	// plane test: critical point c and d1, d2  (:90-95)
 	const float cxp = S.nx > 0.0f ? unit[0] : 0.0f;
