@@ -13,8 +13,10 @@ Keys beyond the base contract:
                (MEASURED_PEAKS.json), with DRAM traffic from the committed ncu summary when present.
   cpu_baseline the reference CPU algorithm (oracle port, OpenMP with a critical section per bit, as
                src/cpu_voxelizer.cpp runs) on a contiguous 1/32 sample of the same triangles.
-  extras       the triangle-size stress soup (2M triangles at 1024^3) against the reference CUDA kernel
-               rebuilt for sm_103a, and the 256-mesh batched workload against plain per-mesh calls.
+  extras       the triangle-size stress soup (2M triangles at 1024^3; the reference CUDA kernel rebuilt
+               for sm_103a is timed on it by --impl reference), the 256-mesh batched workload against
+               plain per-mesh calls, and open-loop serving of that mix (Poisson arrivals, 40 GiB
+               budget, p50/p99) against one-request-at-a-time launches.
 
 --impl reference times the reference's CPU implementation of the path (the oracle port on hosts
 where the reference's own x86 build cannot run) on a bounded sample of the same workload.
@@ -46,7 +48,9 @@ def parse():
     p.add_argument("--steps", type=int, default=400)
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    p.add_argument("--no-extras", action="store_true", help="skip the soup / batch side measurements")
+    p.add_argument("--no-extras", action="store_true", help="skip the soup / batch / serve side measurements")
+    p.add_argument("--serve-seconds", type=float, default=2.0,
+                   help="length of each open-loop serving run (the full served configuration uses 60)")
     return p.parse_args()
 
 
@@ -211,6 +215,13 @@ def run_reference_arm(args, rank, world):
                        "sample_triangles": n},
             "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": threads, "kind": kind, "sample": desc},
             "e2e": {"value": value, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_extras:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                line["extras"] = {"soup_1024_ref_cuda": ref_cuda_soup()}
+        except Exception as e:  # reference kernels not built on this host
+            line["extras"] = {"soup_1024_ref_cuda": f"unavailable: {e}"}
     print(json.dumps(line), flush=True)
 
 
@@ -320,7 +331,7 @@ def main():
     e2e = {"value": world * 4 * T / (e2e_ms / 1e3) / 1e6, "unit": "Mtris/s", "ms_per_step": e2e_ms,
            "h2d_bytes_per_step": int(tris.nbytes), "d2h_bytes_per_step": int(4 * W * 4)}
 
-    # ---- parity spot check of what was timed (against the oracle's reference CPU algorithm) -------
+    # ---- the JSON line; the reference CPU baseline and the side measurements on rank 0 -----------
     extras = {}
     line = {"metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -342,7 +353,10 @@ def main():
                                           "OpenMP parallel-for with a critical section per bit"}
         if not args.no_extras:
             extras.update(bench_soup(cv, meshgen, torch, stream, flush))
-            extras.update(bench_batch(cv, meshgen, torch, stream))
+            specs = meshgen.batch_mix(0, 256)
+            mix = [(s, s.build()) for s in specs]
+            extras.update(bench_batch(cv, torch, mix))
+            extras.update(bench_serve(cv, meshgen, torch, mix, args.serve_seconds))
         line["extras"] = extras
         print(json.dumps(line), flush=True)
 
@@ -373,31 +387,44 @@ def bench_soup(cv, meshgen, torch, stream, flush):
         torch.cuda.synchronize()
         ts.append(a.elapsed_time(b))
     eng_ms = float(np.median(ts))
-    out["soup_1024"] = {"triangles": 2_000_000, "engine_ms": eng_ms, "engine_mtris_s": 2.0 / (eng_ms / 1e3)}
-    try:
-        import oracle
-        ref = oracle.RefGPU()
-        ref_tab = torch.zeros_like(tab)
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        ref.voxelize(bytes(info), d.data_ptr(), ref_tab.data_ptr(), False, False, stream.cuda_stream)
-        b.record(stream)
-        torch.cuda.synchronize()
-        rms = a.elapsed_time(b)
-        out["soup_1024"].update({"ref_cuda_ms": rms, "speedup_vs_ref_cuda": rms / eng_ms,
-                                 "bit_exact_vs_ref_cuda": bool(torch.equal(tab, ref_tab))})
-    except Exception as e:  # reference cubins absent
-        out["soup_1024"]["ref_cuda"] = f"unavailable: {e}"
+    out["soup_1024"] = {"triangles": 2_000_000, "engine_ms": eng_ms, "engine_mtris_s": 2.0 / (eng_ms / 1e3),
+                        "ref_cuda": "timed by --impl reference (extras.soup_1024_ref_cuda)"}
     return out
 
 
-def bench_batch(cv, meshgen, torch, stream):
+def ref_cuda_soup():
+    """The reference CUDA surface kernel (its own source built for sm_103a) on the 2M-triangle soup
+    at 1024^3, one timed launch after one warm-up on a small mesh."""
+    import torch
+    import oracle
+    import cuda_voxelizer_gb300 as cv
+    from cuda_voxelizer_gb300 import meshgen
+    stream = torch.cuda.current_stream()
+    ref = oracle.RefGPU()
+    small = meshgen.torus(0)
+    si = cv.make_voxinfo(small, 64)
+    ds = torch.from_numpy(small.reshape(-1)).cuda()
+    st = torch.zeros(cv.table_words(si), dtype=torch.int32, device="cuda")
+    ref.voxelize(bytes(si), ds.data_ptr(), st.data_ptr(), False, False, stream.cuda_stream)
+    tris = meshgen.soup(0, n=2_000_000)
+    info = cv.make_voxinfo(tris, 1024)
+    d = torch.from_numpy(tris.reshape(-1)).cuda()
+    tab = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ref.voxelize(bytes(info), d.data_ptr(), tab.data_ptr(), False, False, stream.cuda_stream)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    return {"triangles": 2_000_000, "ref_cuda_ms": ms, "ref_cuda_mtris_s": 2.0 / (ms / 1e3)}
+
+
+def bench_batch(cv, torch, mix):
     """256-mesh uneven mix: one graph launch (plan) vs plain per-mesh synchronous calls."""
-    specs = meshgen.batch_mix(0, 256)
     jobs = []
-    for s in specs:
-        t = s.build()
+    for s, t in mix:
         info = cv.make_voxinfo(t, s.gridsize)
         jobs.append(cv.Job(info, torch.from_numpy(t.reshape(-1)).cuda(),
                            torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda"), s.morton, s.solid))
@@ -427,6 +454,50 @@ def bench_batch(cv, meshgen, torch, stream):
     return {"batch_256": {"meshes": 256, "triangles": n_tris, "plan_ms": plan_s * 1e3, "plain_ms": plain_s * 1e3,
                           "plan_meshes_s": 256 / plan_s, "plain_meshes_s": 256 / plain_s,
                           "speedup_vs_plain": plain_s / plan_s}}
+
+
+def bench_serve(cv, meshgen, torch, mix, seconds):
+    """Open-loop serving of the 256-mesh distribution: Poisson arrivals, 40 GiB budget, host buffers
+    in and out.  Capacity is measured with a burst (every request due at t=0); the Poisson sweep then
+    runs at fractions of it.  The plain arm is the same server limited to one request at a time on
+    one stream, i.e. one synchronous per-request launch after another."""
+    pool, keep = [], []
+    for s, t in mix:
+        info = cv.make_voxinfo(t, s.gridsize)
+        h_t = torch.from_numpy(t.reshape(-1)).pin_memory()
+        h_tab = torch.empty(cv.table_words(info), dtype=torch.int32).pin_memory()
+        keep.append((h_t, h_tab))
+        pool.append(cv.Server.request(info, h_t, h_tab, s.morton, s.solid))
+    rng = np.random.default_rng(7)
+
+    def burst(srv, n):
+        lat = srv.replay(pool, rng.integers(0, len(pool), n), np.zeros(n))
+        return n / (float(lat.max()) / 1e3)
+
+    def poisson(srv, rate, seed):
+        arr = meshgen.poisson_arrivals(rate, seconds, seed=seed)
+        lat = srv.replay(pool, rng.integers(0, len(pool), len(arr)), arr)
+        span = float(np.max(arr + lat / 1e3))
+        return {"rate_per_s": round(rate, 1), "requests": int(len(arr)), "meshes_s": len(arr) / span,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+
+    out = {"budget_gib": 40, "seconds_per_rate": seconds, "pool": "256-mesh mix (same as batch_256)",
+           "host_buffers": "pinned, triangles in and table out per request"}
+    with cv.Server(memory_budget_bytes=40 << 30, max_batch=256, max_inflight=4) as srv:
+        burst(srv, 512)
+        cap = burst(srv, 4096)
+        out["served"] = {"capacity_meshes_s": cap, "max_batch": 256, "max_inflight": 4,
+                         "sweep": [poisson(srv, f * cap, i) for i, f in enumerate((0.25, 0.5, 0.75, 0.9))]}
+        st = srv.stats()
+        out["served"]["mean_batch"] = st["mean_batch"]
+        out["served"]["memory_peak_gib"] = st["memory_peak"] / 2 ** 30
+    with cv.Server(memory_budget_bytes=40 << 30, max_batch=1, max_inflight=1) as srv:
+        burst(srv, 64)
+        pcap = burst(srv, 512)
+        out["plain"] = {"capacity_meshes_s": pcap,
+                        "sweep": [poisson(srv, f * pcap, 10 + i) for i, f in enumerate((0.5, 0.9))]}
+    out["served_vs_plain_capacity"] = cap / pcap
+    return {"serve": out}
 
 
 if __name__ == "__main__":

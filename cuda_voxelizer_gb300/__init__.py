@@ -4,10 +4,11 @@ Forceflow/cuda_voxelizer, implemented as hand-written sm_103a CUDA behind a C AB
 The native library ``_lib/libcvx.so`` is required; importing this package without it raises
 ImportError.
 """
-from .api import (CvxError, Job, Plan, VoxInfo, create_mesh_bbox_cube, device_status, get_tuning, make_info,
-                  make_voxinfo, mesh_bbox, profile_collect, profile_enable, set_tuning, table_words, voxelize, voxelize_batch, voxelize_host,
-                  voxelize_solid, voxelize_ws, workspace_size)
+from .api import (CvxError, Job, Plan, Server, VoxInfo, create_mesh_bbox_cube, device_status, get_tuning,
+                  make_info, make_voxinfo, mesh_bbox, profile_collect, profile_enable, set_tuning, table_words,
+                  voxelize, voxelize_batch, voxelize_host, voxelize_solid, voxelize_ws, workspace_size)
 
-__all__ = ["CvxError", "Job", "Plan", "VoxInfo", "create_mesh_bbox_cube", "device_status", "get_tuning",
-           "make_info", "make_voxinfo", "mesh_bbox", "profile_collect", "profile_enable", "set_tuning", "table_words", "voxelize", "voxelize_batch",
-           "voxelize_host", "voxelize_solid", "voxelize_ws", "workspace_size"]
+__all__ = ["CvxError", "Job", "Plan", "Server", "VoxInfo", "create_mesh_bbox_cube", "device_status", "get_tuning",
+           "make_info", "make_voxinfo", "mesh_bbox", "profile_collect", "profile_enable", "set_tuning",
+           "table_words", "voxelize", "voxelize_batch", "voxelize_host", "voxelize_solid", "voxelize_ws",
+           "workspace_size"]

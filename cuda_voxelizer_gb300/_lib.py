@@ -33,6 +33,21 @@ class CvxJob(ctypes.Structure):
                 ("solid", ctypes.c_int32)]
 
 
+class CvxServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", u64), ("max_batch", u32), ("max_inflight", u32)]
+
+
+class CvxServerRequest(ctypes.Structure):
+    _fields_ = [("info", CvxVoxinfo), ("h_triangles", vp), ("h_table", vp), ("morton", ctypes.c_int32),
+                ("solid", ctypes.c_int32)]
+
+
+class CvxServerStats(ctypes.Structure):
+    _fields_ = [("completed", u64), ("pending", u64), ("batches", u64), ("mean_batch", ctypes.c_double),
+                ("memory_used", u64), ("memory_budget", u64), ("memory_peak", u64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("meshes_per_s", ctypes.c_double)]
+
+
 class CvxTuning(ctypes.Structure):
     _fields_ = [("small_vox", ctypes.c_uint32), ("small_cols", ctypes.c_uint32)]
 
@@ -58,6 +73,13 @@ SIGNATURES = {
     "cvx_plan_create": (c_status, [ctypes.POINTER(CvxJob), u32, u32, ctypes.POINTER(vp)]),
     "cvx_plan_launch": (c_status, [vp, vp]),
     "cvx_plan_destroy": (c_status, [vp]),
+    "cvx_server_create": (c_status, [ctypes.POINTER(CvxServerConfig), ctypes.POINTER(vp)]),
+    "cvx_server_submit": (c_status, [vp, ctypes.POINTER(CvxServerRequest), ctypes.POINTER(u64)]),
+    "cvx_server_wait": (c_status, [vp, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "cvx_server_stats_get": (c_status, [vp, ctypes.POINTER(CvxServerStats)]),
+    "cvx_server_replay": (c_status, [vp, ctypes.POINTER(CvxServerRequest), u32, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double)]),
+    "cvx_server_destroy": (c_status, [vp]),
     "cvx_get_tuning": (c_status, [ctypes.c_int, ctypes.POINTER(CvxTuning)]),
     "cvx_set_tuning": (c_status, [ctypes.c_int, ctypes.POINTER(CvxTuning)]),
     "cvx_profile_enable": (c_status, [ctypes.c_int]),

@@ -15,11 +15,12 @@ from typing import Sequence
 
 import numpy as np
 
-from ._lib import CvxError, CvxJob, CvxTuning, CvxVoxinfo, check, lib
+from ._lib import (CvxError, CvxJob, CvxServerConfig, CvxServerRequest, CvxServerStats, CvxTuning, CvxVoxinfo,
+                   check, lib)
 
 __all__ = ["VoxInfo", "voxelize", "voxelize_solid", "voxelize_ws", "workspace_size", "create_mesh_bbox_cube",
            "mesh_bbox", "make_voxinfo", "table_words", "Job", "voxelize_batch", "Plan", "device_status",
-           "get_tuning", "set_tuning", "CvxError", "voxelize_host", "profile_enable", "profile_collect"]
+           "get_tuning", "set_tuning", "CvxError", "voxelize_host", "profile_enable", "profile_collect", "Server"]
 
 
 VoxInfo = CvxVoxinfo
@@ -223,3 +224,101 @@ def voxelize_host(info: VoxInfo, triangles: np.ndarray, morton: bool = False, so
     table = torch.zeros(table_words(info), dtype=torch.int32, device="cuda")
     (voxelize_solid if solid else voxelize)(info, t, table, morton)
     return table.cpu().numpy().view(np.uint32)
+
+
+def _host_ptr(x, writable: bool) -> int:
+    """Address of a contiguous host buffer (numpy array or CPU tensor; pinned memory lets the
+    server's copies overlap with other batches)."""
+    if hasattr(x, "data_ptr"):
+        if x.is_cuda:
+            raise ValueError("server requests take host buffers")
+        if not x.is_contiguous():
+            raise ValueError("host buffers must be contiguous")
+        return int(x.data_ptr())
+    if not isinstance(x, np.ndarray) or not x.flags.c_contiguous or (writable and not x.flags.writeable):
+        raise ValueError("host buffers must be C-contiguous numpy arrays (writable for the table) or CPU tensors")
+    return int(x.ctypes.data)
+
+
+def _host_nbytes(x) -> int:
+    return x.numel() * x.element_size() if hasattr(x, "numel") else x.nbytes
+
+
+class Server:
+    """Voxelization server (cvx_server_*): requests are admitted by the device memory they need out
+    of a fixed budget and batched continuously on ``max_inflight`` streams.  Each request reads its
+    triangles from a host buffer and writes its table to a host buffer; both must stay alive until
+    the request has been waited for."""
+
+    def __init__(self, memory_budget_bytes: int = 40 << 30, max_batch: int = 256, max_inflight: int = 4):
+        cfg = CvxServerConfig(int(memory_budget_bytes), int(max_batch), int(max_inflight))
+        h = ctypes.c_void_p()
+        check(lib.cvx_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cvx_server_create")
+        self._h = h
+        self._keep = {}
+
+    @staticmethod
+    def request(info: VoxInfo, triangles, table, morton_code: bool = False, solid: bool = False) -> CvxServerRequest:
+        if _host_nbytes(triangles) < 36 * info.n_triangles:
+            raise ValueError("triangle buffer smaller than 9 floats per triangle")
+        if _host_nbytes(table) < 4 * table_words(info):
+            raise ValueError(f"table buffer smaller than {4 * table_words(info)} bytes")
+        return CvxServerRequest(info, _host_ptr(triangles, False), _host_ptr(table, True), int(bool(morton_code)),
+                                int(bool(solid)))
+
+    def submit(self, info: VoxInfo, triangles, table, morton_code: bool = False, solid: bool = False) -> int:
+        req = self.request(info, triangles, table, morton_code, solid)
+        rid = ctypes.c_uint64()
+        check(lib.cvx_server_submit(self._h, ctypes.byref(req), ctypes.byref(rid)), "cvx_server_submit")
+        self._keep[rid.value] = (triangles, table)
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: float = -1.0) -> float:
+        """Waits for request ``rid``; returns its latency in ms (submission to table written)."""
+        lat = ctypes.c_double()
+        st = lib.cvx_server_wait(self._h, int(rid), float(timeout_ms), ctypes.byref(lat))
+        if not (st == 1 and b"timed out" in lib.cvx_last_error_message()):
+            self._keep.pop(int(rid), None)
+        check(st, "cvx_server_wait")
+        return lat.value
+
+    def stats(self) -> dict:
+        s = CvxServerStats()
+        check(lib.cvx_server_stats_get(self._h, ctypes.byref(s)), "cvx_server_stats_get")
+        return {k: getattr(s, k) for k, _ in CvxServerStats._fields_}
+
+    def replay(self, pool: Sequence[CvxServerRequest], index, arrival_s) -> np.ndarray:
+        """Open-loop load: request i is ``pool[index[i]]``, submitted at ``arrival_s[i]`` seconds
+        (ascending) after the call starts.  Returns per-request latency in ms, counted from the
+        scheduled arrival.  The pool's buffers must stay alive during the call."""
+        index = np.asarray(index, dtype=np.int64)
+        arrival = np.ascontiguousarray(arrival_s, dtype=np.float64)
+        if index.shape != arrival.shape:
+            raise ValueError("index and arrival_s differ in length")
+        size = ctypes.sizeof(CvxServerRequest)
+        pool_arr = (CvxServerRequest * len(pool))(*pool)
+        rows = np.frombuffer(pool_arr, dtype=np.uint8).reshape(len(pool), size)
+        reqs = np.ascontiguousarray(rows[index])
+        lat = np.zeros(len(index), dtype=np.float64)
+        dp = ctypes.POINTER(ctypes.c_double)
+        check(lib.cvx_server_replay(self._h, reqs.ctypes.data_as(ctypes.POINTER(CvxServerRequest)), len(index),
+                                    arrival.ctypes.data_as(dp), lat.ctypes.data_as(dp)), "cvx_server_replay")
+        return lat
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.cvx_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

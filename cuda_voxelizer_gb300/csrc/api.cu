@@ -439,7 +439,61 @@ cvx_status run_internal(std::vector<JobDesc> surf, std::vector<JobDesc> solid, c
 	return CVX_OK;
 }
 
+// Job descriptors of a cvx_job array, split by mode (empty jobs dropped); flips[i], if given,
+// becomes job i's flip table.
+cvx_status collect_jobs(const cvx_job* jobs, uint32_t n_jobs, uint32_t* const* flips, std::vector<JobDesc>& surf,
+                        std::vector<JobDesc>& solid) {
+	if (n_jobs && !jobs) return fail(CVX_ERR_INVALID_VALUE, "jobs is null");
+	for (uint32_t i = 0; i < n_jobs; i++) {
+		cvx_status st = validate(&jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton);
+		if (st != CVX_OK) return fail(st, "job %u: %s", i, g_msg.c_str());
+		if (jobs[i].info.n_triangles == 0) continue;
+		JobDesc j = make_job(jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
+		if (flips && jobs[i].solid) {
+			if (!flips[i]) return fail(CVX_ERR_INVALID_VALUE, "job %u: no flip table", i);
+			j.flips = flips[i];
+		}
+		(jobs[i].solid ? solid : surf).push_back(j);
+	}
+	return CVX_OK;
+}
+
 }  // namespace
+
+cvx_status cvx::batch_scratch_bytes(const cvx_job* jobs, uint32_t n_jobs, size_t* rec_bytes, size_t* staging_bytes) {
+	std::vector<JobDesc> surf, solid;
+	cvx_status st = collect_jobs(jobs, n_jobs, nullptr, surf, solid);
+	if (st != CVX_OK) return st;
+	const size_t slots = job_slots(surf, solid);
+	*rec_bytes = rec_layout(queue_cap(surf, solid), slots).end;
+	*staging_bytes = std::max<size_t>(slots, 1) * sizeof(JobDesc);
+	return CVX_OK;
+}
+
+cvx_status cvx::run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* const* flips, void* d_rec,
+                             size_t rec_bytes, void* h_staging, size_t staging_bytes, cudaStream_t s) {
+	std::vector<JobDesc> surf, solid;
+	cvx_status st = collect_jobs(jobs, n_jobs, flips, surf, solid);
+	if (st != CVX_OK) return st;
+	if (surf.empty() && solid.empty()) return CVX_OK;
+	if (!solid.empty() && !flips) return fail(CVX_ERR_INVALID_VALUE, "solid jobs need flip tables");
+	const uint64_t cap = queue_cap(surf, solid);
+	const size_t slots = job_slots(surf, solid);
+	const RecLayout lay = rec_layout(cap, slots);
+	if (!d_rec || rec_bytes < lay.end || reinterpret_cast<uintptr_t>(d_rec) % kAlign)
+		return fail(CVX_ERR_INVALID_VALUE, "record area too small or not 256-byte aligned");
+	if (slots && (!h_staging || staging_bytes < slots * sizeof(JobDesc)))
+		return fail(CVX_ERR_INVALID_VALUE, "job staging too small");
+	DevState dev;
+	st = dev_state(dev);
+	if (st != CVX_OK) return st;
+	Runner r{s, dev, static_cast<char*>(d_rec), lay.end, nullptr, static_cast<JobDesc*>(h_staging),
+	         staging_bytes / sizeof(JobDesc)};
+	r.cap = cap;
+	r.jobs_off = lay.jobs;
+	CVX_CUDA(cudaMemsetAsync(d_rec, 0, sizeof(Counters), s));
+	return r.run(surf, solid);
+}
 
 void cvx::set_message(const std::string& m) { g_msg = m; }
 
@@ -627,6 +681,7 @@ struct cvx_plan {
 	void* rec = nullptr;
 	uint32_t* flips = nullptr;
 	JobDesc* staging = nullptr;
+	ClearRange* clears = nullptr;  // the tables the graph zeroes (CVX_PLAN_CLEAR_TABLES)
 };
 
 cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out) {
@@ -670,6 +725,23 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 	}
 	if (slots && cudaMallocHost((void**)&p->staging, slots * sizeof(JobDesc)) != cudaSuccess)
 		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan staging"));
+	std::vector<ClearRange> clears;
+	uint32_t clear_total = 0;
+	if (flags & CVX_PLAN_CLEAR_TABLES) {
+		for (auto& t : tables) {
+			clears.push_back(ClearRange{t.first, t.second, clear_total, 0u});
+			clear_total += clear_chunks(t.second);
+		}
+		if (!clears.empty()) {
+			if (cudaMalloc((void**)&p->clears, clears.size() * sizeof(ClearRange)) != cudaSuccess) {
+				cudaGetLastError();
+				return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan clear list"));
+			}
+			if (cudaMemcpy(p->clears, clears.data(), clears.size() * sizeof(ClearRange), cudaMemcpyHostToDevice) !=
+			    cudaSuccess)
+				return bail(cuda_fail(cudaGetLastError(), "clear list upload"));
+		}
+	}
 	cudaStream_t cs;
 	if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "stream"));
 	// Upload the job arrays once, outside the graph (the graph only reads them), in the order the
@@ -702,10 +774,8 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		return bail(cuda_fail(cudaGetLastError(), "begin capture"));
 	}
 	cvx_status cst = CVX_OK;
-	if (flags & CVX_PLAN_CLEAR_TABLES)
-		for (auto& t : tables)
-			if (cst == CVX_OK && cudaMemsetAsync(t.first, 0, t.second * 4, cs) != cudaSuccess)
-				cst = cuda_fail(cudaGetLastError(), "table clear");
+	if (!clears.empty() && launch_clear(p->clears, (uint32_t)clears.size(), clear_total, cs) != cudaSuccess)
+		cst = cuda_fail(cudaGetLastError(), "table clear");
 	if (cst == CVX_OK && cudaMemsetAsync(p->rec, 0, sizeof(Counters), cs) != cudaSuccess)
 		cst = cuda_fail(cudaGetLastError(), "counter clear");
 	if (cst == CVX_OK) {
@@ -787,6 +857,7 @@ cvx_status cvx_plan_destroy(cvx_plan* p) {
 	if (p->rec) cudaFree(p->rec);
 	if (p->flips) cudaFree(p->flips);
 	if (p->staging) cudaFreeHost(p->staging);
+	if (p->clears) cudaFree(p->clears);
 	delete p;
 	return CVX_OK;
 }

@@ -106,6 +106,33 @@ struct Counters {
 };
 constexpr size_t kCountersResetBytes = 20;  // big, ticket, mid: reset before every launch sequence
 
+// Work tickets of the cooperative kernels, claimed by a warp K at a time: one atomic on the shared
+// counter per K items instead of per item (a single hot address serialises in its L2 slice when
+// hundreds of thousands of small items are queued).  K grows with the items per warp, up to 16,
+// so the tail left when the counter runs out stays short.
+struct WarpTickets {
+	unsigned long long next = 0, end = 0;
+	uint32_t K;
+	__device__ WarpTickets(uint64_t total, uint32_t n_warps) {
+		const uint64_t per = total / ((uint64_t)n_warps * 8u);
+		K = (uint32_t)(per < 1 ? 1 : (per > 16 ? 16 : per));
+	}
+	// Next ticket of this warp (the same in every lane); false once every ticket is claimed.
+	__device__ __forceinline__ bool take(unsigned long long* ctr, uint64_t total, uint32_t lane,
+	                                     unsigned long long& tk) {
+		if (next >= end) {
+			unsigned long long b = 0;
+			if (lane == 0) b = atomicAdd(ctr, (unsigned long long)K);
+			b = __shfl_sync(0xFFFFFFFFu, b, 0);
+			next = b;
+			end = b + K;
+		}
+		if (next >= total) return false;
+		tk = next++;
+		return true;
+	}
+};
+
 struct Scratch {
 	Counters* ctr;
 	BigRec* big;

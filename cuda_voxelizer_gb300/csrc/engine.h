@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <string>
+#include "cvx.h"
 #include "cvx_device.cuh"
 
 namespace cvx {
@@ -11,7 +12,8 @@ constexpr uint32_t kTile = 256;        // triangles per classify CTA (one tile)
 constexpr uint32_t kZch = 32;          // z-slices per surface work item (one per lane)
 constexpr uint32_t kRowsThreads = 256; // threads per cooperative CTA
 constexpr uint32_t kColsPerItem = 256; // solid columns per work item
-constexpr uint32_t kSmallRows = 16;    // surface: rows of a triangle handled in the classify kernel
+constexpr uint32_t kSmallRows = 16;    // surface: rows of a small triangle (every voxel tested)
+constexpr uint32_t kLocalRows = 64;    // surface: rows of a local triangle (row intervals), classify kernel
 constexpr uint32_t kSmallCols = 16;    // solid: columns of a triangle handled in the classify kernel
 
 // Device-side check codes written to Counters::error.
@@ -58,7 +60,28 @@ struct SolidUnits {
 };
 SolidUnits solid_units(const uint32_t grid[3]);
 
+// Zeroing many tables in one launch: ranges sorted by chunk_begin, the prefix sum of
+// clear_chunks(words) over the ranges before them.
+struct ClearRange {
+	uint32_t* ptr;
+	uint64_t words;
+	uint32_t chunk_begin;
+	uint32_t pad;
+};
+constexpr uint32_t kClearChunkWords = 16384;  // 64 KiB per CTA
+uint32_t clear_chunks(uint64_t words);
+cudaError_t launch_clear(const ClearRange* d_ranges, uint32_t n, uint32_t total_chunks, cudaStream_t s);
+
 // Sets the message returned by cvx_last_error_message() on this host thread.
 void set_message(const std::string& m);
+
+// A batch run on caller-owned memory (used by the server, whose memory all comes from its budget).
+// batch_scratch_bytes gives the device record bytes (256-byte aligned) and the pinned host staging
+// bytes that run_batch_on needs for `jobs`.  run_batch_on takes one flip table per job in `flips`
+// (read for solid jobs only: table-sized, zero on entry, zero again afterwards); the staging buffer
+// must stay untouched until the stream has passed this call.
+cvx_status batch_scratch_bytes(const cvx_job* jobs, uint32_t n_jobs, size_t* rec_bytes, size_t* staging_bytes);
+cvx_status run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* const* flips, void* d_rec, size_t rec_bytes,
+                        void* h_staging, size_t staging_bytes, cudaStream_t s);
 
 }  // namespace cvx

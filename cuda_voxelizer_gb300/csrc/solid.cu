@@ -376,11 +376,10 @@ __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant
 	// Warps beyond the number of queued items have nothing to claim: they leave without touching
 	// the ticket counter (all of them do when only small triangles were queued).
 	if ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) >= total) return;
+	WarpTickets wt(total, gridDim.x * (blockDim.x >> 5));
 	for (;;) {
 		unsigned long long tk = 0;
-		if (lane == 0) tk = atomicAdd(&C->ticket, 1ull);
-		tk = __shfl_sync(FULL, tk, 0);
-		if (tk >= total) break;
+		if (!wt.take(&C->ticket, total, lane, tk)) break;
 		uint32_t job = 0, tri = 0, chunk = 0, ok = 0;
 		if (lane == 0) {
 			if (tk < n_big_items) {

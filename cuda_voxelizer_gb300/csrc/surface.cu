@@ -5,9 +5,10 @@
 //   surf_classify  one CTA per tile of 256 triangles of one job.  The tile is staged into shared
 //                  memory with one cp.async.bulk (TMA bulk copy) when it is full and 16-byte
 //                  aligned.  Each thread sets up its triangle; triangles whose grid bbox holds at
-//                  most `small_vox` voxels are finished in the thread (every voxel of the bbox
-//                  tested, like the reference); the others are queued, one record per triangle,
-//                  as one item ("mid") or as one item per 32 z-slices ("big").
+//                  most `small_vox` voxels (every voxel tested, like the reference) or at most
+//                  kLocalRows rows (row intervals) are finished by the CTA, their rows dealt over
+//                  its threads; the others are queued, one record per triangle, as one item
+//                  ("mid") or as one item per 32 z-slices ("big").
 //   surf_rows      persistent CTAs; each warp takes work tickets (big items first, then mid
 //                  triangles), finds the y-interval of every z-slice of the item (one lane per
 //                  slice), flattens the (y, z) rows and gives one row per lane; each lane finds the
@@ -112,18 +113,22 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uin
 	return (warp ? s_warp[warp - 1] : 0u) + incl - v;
 }
 
-// Phase 1: one thread per triangle (setup, classify, queue the big ones, park the small ones'
-// setup in shared memory).  Phase 2: the rows of all small triangles of the tile are dealt out
-// evenly over the CTA, one (triangle, row) item per thread at a time, so that no thread idles while
-// another walks a larger bounding box.
+// Phase 1: one thread per triangle: setup, then one of three bins.  Small triangles (a few voxels)
+// and local ones (at most kLocalRows rows, extents below 256) park their setup in shared memory;
+// the rest are queued for surf_rows.  Phase 2: the rows of the tile's small and local triangles
+// are dealt out evenly over the CTA, one (triangle, row) item per thread at a time, so that no
+// thread idles while another walks a larger bounding box.  A small triangle's row tests every
+// voxel like the reference; a local triangle's row is found with row_interval.
 template <class P>
-__global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_vox) {
+__global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_vox) {
 	__shared__ __align__(16) union {
 		float tri[kTile * 9];
 		SmallTri small[kTile];
 	} sm;
-	__shared__ uint16_t s_items[kTile * kSmallRows];  // (triangle | dy << 8 | dz << 12) per row
+	// per row: small triangle | dy << 8 | dz << 12, or local triangle | row << 8
+	__shared__ uint16_t s_items[kTile * kSmallRows];
 	__shared__ uint32_t s_warp[kTile / 32];
+	__shared__ uint32_t s_fit;  // end of the item list: the first local triangle that did not fit
 	__shared__ __align__(8) uint64_t s_bar;
 	const uint32_t tile = blockIdx.x;
 	const uint32_t j = job_of_tile(L, tile);
@@ -148,20 +153,38 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 	__syncthreads();  // the tile is consumed; its shared memory now holds SmallTri records
 
 	bool is_mid = false, is_big = false;
-	uint32_t n_items = 0, n_rows = 0;
+	uint32_t n_items = 0, n_small = 0, n_local = 0;
 	if (valid) {
 		SurfTri S;
 		surf_setup<P>(t, bmin, unit, inv, grid, S);
-		const uint64_t rows = (uint64_t)(S.by1 - S.by0 + 1) * (uint64_t)(S.bz1 - S.bz0 + 1);
-		const uint64_t nvox = (uint64_t)(S.bx1 - S.bx0 + 1) * rows;
-		if (nvox <= small_vox && nvox <= 255 && rows <= kSmallRows && S.by1 - S.by0 < 16 && S.bz1 - S.bz0 < 16) {
+		const uint32_t ex = (uint32_t)(S.bx1 - S.bx0), ey = (uint32_t)(S.by1 - S.by0), ez = (uint32_t)(S.bz1 - S.bz0);
+		const uint64_t rows = (uint64_t)(ey + 1) * (uint64_t)(ez + 1);
+		const uint64_t nvox = (uint64_t)(ex + 1) * rows;
+		if (nvox <= small_vox && nvox <= 255 && rows <= kSmallRows && ey < 16 && ez < 16) {
 			pack_small(S, sm.small[threadIdx.x]);
-			n_rows = (uint32_t)rows;
+			n_small = (uint32_t)rows;
 		} else {
-			n_items = (uint32_t)((S.bz1 - S.bz0 + kZch) / kZch);
-			is_mid = n_items == 1;
-			is_big = n_items > 1;
+			n_items = (ez + kZch) / kZch;
+			if (rows <= kLocalRows && ex < 256 && ey < 256 && ez < 256) {
+				pack_small(S, sm.small[threadIdx.x]);
+				n_local = (uint32_t)rows;
+			}
 		}
+	}
+	// One item list for the tile: the rows of the small triangles, then those of the local ones.
+	// A local triangle whose rows no longer fit is queued like the larger ones.
+	if (threadIdx.x == 0) s_fit = 0xFFFFFFFFu;  // ordered before the atomics by the scan's barriers
+	uint32_t totals = 0;
+	const uint32_t offs = block_scan(n_small | (n_local << 16), s_warp, &totals);
+	const uint32_t total_small = totals & 0xFFFFu;
+	const uint32_t loff = total_small + (offs >> 16);
+	if (n_local && loff + n_local > kTile * kSmallRows) {
+		atomicMin(&s_fit, loff);
+		n_local = 0;
+	}
+	if (n_items && !n_local) {
+		is_mid = n_items == 1;
+		is_big = n_items > 1;
 	}
 	// Queue the other triangles: warp-aggregated appends.
 	const uint32_t lt = (1u << lane) - 1u;
@@ -200,34 +223,55 @@ __global__ void __launch_bounds__(kTile) surf_classify(const __grid_constant__ L
 		}
 	}
 
-	// Phase 2: rows of the small triangles (src/voxelize.cu:136-183, every voxel of each row).
-	uint32_t total_rows = 0;
-	const uint32_t off = block_scan(n_rows, s_warp, &total_rows);
-	if (n_rows) {
+	// Phase 2: the rows of the tile's small and local triangles, dealt evenly over the CTA.
+	if (n_small) {
 		const SmallTri& o = sm.small[threadIdx.x];
 		const uint32_t ny = ((o.ext >> 8) & 0xFFu) + 1u;
-		for (uint32_t r = 0; r < n_rows; r++)
+		const uint32_t off = offs & 0xFFFFu;
+		for (uint32_t r = 0; r < n_small; r++)
 			s_items[off + r] = (uint16_t)(threadIdx.x | ((r % ny) << 8) | ((r / ny) << 12));
 	}
+	for (uint32_t r = 0; r < n_local; r++) s_items[loff + r] = (uint16_t)(threadIdx.x | (r << 8));
 	__syncthreads();
-	for (uint32_t k = threadIdx.x; k < total_rows; k += kTile) {
+	const uint32_t total_items = min(total_small + (totals >> 16), s_fit);
+	for (uint32_t k = threadIdx.x; k < total_items; k += kTile) {
 		const uint32_t it = s_items[k];
 		SurfTri S;
 		unpack_small(sm.small[it & 0xFFu], S);
-		const int y = S.by0 + (int)((it >> 8) & 0xFu), z = S.bz0 + (int)(it >> 12);
+		const bool small = k < total_small;
+		int y, z;
+		if (small) {
+			y = S.by0 + (int)((it >> 8) & 0xFu);
+			z = S.bz0 + (int)(it >> 12);
+		} else {
+			// row r of a local triangle: r = dy + dz * ny with r < kLocalRows and ny < 256, so the
+			// approximate quotient is more than 1e-3 away from the next integer and truncates exactly
+			const uint32_t r = it >> 8, ny = (uint32_t)(S.by1 - S.by0) + 1u;
+			const uint32_t dz = (uint32_t)__fdividef((float)r + 0.5f, (float)ny);
+			y = S.by0 + (int)(r - dz * ny);
+			z = S.bz0 + (int)dz;
+		}
 		const float py = __fmul_rn(__int2float_rn(y), unit[1]);
 		const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
 		if (yz_fail_bits<P>(S, py, pz)) continue;
 		RowK K;
 		row_consts<P>(S, py, pz, K);
-		WordSink sink{table};
-		const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
-		const uint64_t yzm = morton ? ((spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2)) : 0;
-		for (int x = S.bx0; x <= S.bx1; x++) {
-			if (!voxel_pass<P>(S, K, unit[0], x)) continue;
-			sink.add(morton ? (spread3((uint32_t)x) | yzm) : base + (uint64_t)x);
+		if (small) {
+			// src/voxelize.cu:136-183: every voxel of the row
+			WordSink sink{table};
+			const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
+			const uint64_t yzm = morton ? ((spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2)) : 0;
+			for (int x = S.bx0; x <= S.bx1; x++) {
+				if (!voxel_pass<P>(S, K, unit[0], x)) continue;
+				sink.add(morton ? (spread3((uint32_t)x) | yzm) : base + (uint64_t)x);
+			}
+			sink.flush();
+		} else {
+			RowDirs D;
+			row_dirs(S, unit[0], D);
+			int xl, xh;
+			if (row_interval<P>(S, D, K, unit[0], xl, xh)) write_row(table, morton, grid, y, z, xl, xh);
 		}
-		sink.flush();
 	}
 }
 
@@ -252,11 +296,10 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 	// Warps beyond the number of queued items have nothing to claim: they leave without touching
 	// the ticket counter (all of them do when only small triangles were queued).
 	if ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) >= total) return;
+	WarpTickets wt(total, gridDim.x * (blockDim.x >> 5));
 	for (;;) {
 		unsigned long long tk = 0;
-		if (lane == 0) tk = atomicAdd(&C->ticket, 1ull);
-		tk = __shfl_sync(FULL, tk, 0);
-		if (tk >= total) break;
+		if (!wt.take(&C->ticket, total, lane, tk)) break;
 		uint32_t job = 0, tri = 0, chunk = 0, ok = 0;
 		if (lane == 0) {
 			if (tk < n_big_items) {

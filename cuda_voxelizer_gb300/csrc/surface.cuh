@@ -230,6 +230,8 @@ __device__ __forceinline__ uint32_t yz_fail_bits(const SurfTri& S, float py, flo
 
 // Direction of every x-dependent test for this triangle: lo = passes on a suffix of x (a lower
 // bound), hi = passes on a prefix (an upper bound); tests in neither mask do not depend on x.
+// The reciprocals only steer where the exact walk of row_interval starts, so the fast
+// approximate division is enough (an infinite or NaN estimate falls back to the bbox end).
 struct RowDirs {
 	uint32_t lo, hi;
 	float inv[8];    // -1 / (coefficient of x in the test, in voxels): x* = (row term + d) * inv
@@ -240,15 +242,15 @@ __device__ __forceinline__ void row_dirs(const SurfTri& S, float ux, RowDirs& D)
 	// plane: s increases with x when n.x > 0. "below" (bit 0) then holds on a prefix -> lower bound.
 	if (S.nx > 0.0f) { D.lo |= 1u; D.hi |= 2u; }
 	else if (S.nx < 0.0f) { D.lo |= 2u; D.hi |= 1u; }
-	const float ipl = -1.0f / (S.nx * ux);
+	const float ipl = __fdividef(-1.0f, S.nx * ux);
 	D.inv[0] = ipl; D.inv[1] = ipl;
 #pragma unroll
 	for (int i = 0; i < 3; i++) {
 		const float cxy = S.exy[i][0], czx = S.ezx[i][1];
 		if (cxy > 0.0f) D.lo |= 1u << (2 + i); else if (cxy < 0.0f) D.hi |= 1u << (2 + i);
 		if (czx > 0.0f) D.lo |= 1u << (5 + i); else if (czx < 0.0f) D.hi |= 1u << (5 + i);
-		D.inv[2 + i] = -1.0f / (cxy * ux);
-		D.inv[5 + i] = -1.0f / (czx * ux);
+		D.inv[2 + i] = __fdividef(-1.0f, cxy * ux);
+		D.inv[5 + i] = __fdividef(-1.0f, czx * ux);
 	}
 }
 
@@ -312,7 +314,7 @@ __device__ __forceinline__ bool y_interval(const SurfTri& S, float uy, float pz,
 		const float a = S.eyz[i][0];
 		if (a > 0.0f) lo |= 1u << i; else if (a < 0.0f) hi |= 1u << i;
 		if (a != 0.0f) {
-			const float c = -(S.eyz[i][1] * pz + S.dyz[i]) / (a * uy);
+			const float c = __fdividef(-(S.eyz[i][1] * pz + S.dyz[i]), a * uy);
 			if (a > 0.0f) elo = fmaxf(elo, ceilf(c)); else ehi = fminf(ehi, floorf(c));
 		}
 	}

@@ -133,6 +133,52 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 cvx_status cvx_plan_launch(cvx_plan* plan, cvx_stream_t stream);
 cvx_status cvx_plan_destroy(cvx_plan* plan);
 
+/* ---- serving: requests admitted by device memory and batched continuously --------------------
+ * No counterpart in the reference (src/main.cpp voxelizes one mesh per process).  A server owns
+ * one device arena of memory_budget_bytes (allocated at creation, nothing else is allocated while
+ * serving) holding every admitted request's triangles, table, solid flip table and its batch's
+ * work records, and max_inflight streams.  A worker thread launches pending requests as one
+ * batch (at most max_batch requests, in arrival order, as many as the free budget holds) whenever
+ * a stream is free, so requests that arrive while others run go into the next batch and overlap
+ * with them.  Each request's triangles are copied in and its table copied out within its batch;
+ * host buffers should be pinned (page-locked) for the copies to overlap.  Results are identical
+ * to cvx_voxelize / cvx_voxelize_solid on the same request. */
+typedef struct cvx_server cvx_server;
+typedef struct cvx_server_config {
+	uint64_t memory_budget_bytes;
+	uint32_t max_batch;     /* requests per launch sequence */
+	uint32_t max_inflight;  /* batches on the GPU at once (one stream each) */
+} cvx_server_config;
+typedef struct cvx_server_request {
+	cvx_voxinfo info;
+	const float* h_triangles;  /* 9 floats per triangle; read until the request completes */
+	uint32_t* h_table;         /* cvx_table_words(&info) words, written by the time it completes */
+	int32_t morton;
+	int32_t solid;
+} cvx_server_request;
+typedef struct cvx_server_stats {
+	uint64_t completed, pending, batches;
+	double mean_batch;                    /* requests per batch */
+	uint64_t memory_used, memory_budget;  /* arena bytes now in use / in total */
+	uint64_t memory_peak;                 /* most arena bytes ever in use at once */
+	double p50_ms, p99_ms, max_ms;        /* latency, submission to table written */
+	double meshes_per_s;                  /* completed / (last completion - first submission) */
+} cvx_server_stats;
+/* CVX_ERR_OUT_OF_MEMORY if the budget cannot be allocated. */
+cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out);
+/* Queues one request.  CVX_ERR_OUT_OF_MEMORY if it would not fit even in an empty budget. */
+cvx_status cvx_server_submit(cvx_server* s, const cvx_server_request* req, uint64_t* out_id);
+/* Waits for request `id` (timeout_ms < 0: no limit) and forgets it; returns its status.  A timeout
+ * returns CVX_ERR_INVALID_VALUE and keeps the request. */
+cvx_status cvx_server_wait(cvx_server* s, uint64_t id, double timeout_ms, double* latency_ms);
+cvx_status cvx_server_stats_get(cvx_server* s, cvx_server_stats* out);
+/* Open-loop load: submits reqs[i] at arrival_s[i] seconds after the call starts (arrival_s
+ * ascending), waits for all and writes each latency, counted from its scheduled arrival. */
+cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint32_t n, const double* arrival_s,
+                             double* latency_ms);
+/* Finishes the queued requests, then frees everything. */
+cvx_status cvx_server_destroy(cvx_server* s);
+
 /* ---- tuning ---------------------------------------------------------------------------------- */
 
 typedef struct cvx_tuning {

@@ -100,3 +100,19 @@ def test_mesh_bbox_host():
     assert list(lo) == [0, -4, 2] and list(hi) == [6, 7, 8]
     with pytest.raises(cv.CvxError):
         cv.mesh_bbox(np.zeros((0, 9), np.float32))
+
+
+def test_server_config_validation_answers_without_a_gpu():
+    h = ctypes.c_void_p()
+    for budget, batch, inflight in ((0, 8, 2), (64 << 20, 0, 2), (64 << 20, 8, 0), (64 << 20, 8, 65)):
+        cfg = _lib.CvxServerConfig(budget, batch, inflight)
+        assert _lib.lib.cvx_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert b"budget" in _lib.lib.cvx_last_error_message()
+    assert _lib.lib.cvx_server_submit(None, None, None) == 1
+    assert _lib.lib.cvx_server_destroy(None) == 0
+
+
+def test_server_request_struct_layout():
+    R = _lib.CvxServerRequest
+    assert ctypes.sizeof(R) == 64 + 8 + 8 + 4 + 4
+    assert R.h_triangles.offset == 64 and R.h_table.offset == 72 and R.solid.offset == 84

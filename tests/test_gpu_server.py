@@ -1,0 +1,110 @@
+"""The voxelization server (cvx_server_*): continuous batching under a device-memory budget.
+
+Every result the server returns must be bit-identical to the same request run alone through
+cvx_voxelize / cvx_voxelize_solid (which the parity tests pin to the reference kernels), whatever
+batch it landed in and whatever ran beside it.  Admission must keep the arena within its budget and
+refuse requests that could never fit.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from cuda_voxelizer_gb300 import api as cv  # noqa: E402
+from cuda_voxelizer_gb300 import meshgen  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+GARBAGE = 0x5A5A5A5A  # output buffers start dirty: the server must clear each table itself
+
+
+def _mesh_requests(n, seed, max_tris):
+    out = []
+    for spec in meshgen.batch_mix(seed, 16 * n):
+        if spec.n_triangles <= max_tris:
+            out.append(spec)
+        if len(out) == n:
+            break
+    return out
+
+
+def _host(spec):
+    tris = spec.build()
+    info = cv.make_voxinfo(tris, spec.gridsize)
+    h_tris = torch.from_numpy(tris.reshape(-1).copy()).pin_memory()
+    table = torch.full((cv.table_words(info),), GARBAGE, dtype=torch.int32).pin_memory()
+    return info, h_tris, table
+
+
+def _alone(info, h_tris, morton, solid):
+    t = h_tris.cuda()
+    table = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+    (cv.voxelize_solid if solid else cv.voxelize)(info, t, table, morton)
+    torch.cuda.synchronize()
+    return table.cpu()
+
+
+def test_server_results_identical_alone_and_in_the_mix():
+    specs = _mesh_requests(32, seed=3, max_tris=60_000)
+    assert {s.solid for s in specs} == {False, True} and {s.morton for s in specs} == {False, True}
+    host = [_host(s) for s in specs]
+    with cv.Server(memory_budget_bytes=1 << 30, max_batch=8, max_inflight=3) as srv:
+        ids = [srv.submit(info, t, tab, s.morton, s.solid) for s, (info, t, tab) in zip(specs, host)]
+        lat = [srv.wait(i) for i in ids]
+        st = srv.stats()
+    assert st["completed"] == len(specs) and st["pending"] == 0 and st["memory_used"] == 0
+    assert st["memory_peak"] <= st["memory_budget"]
+    assert all(x > 0 for x in lat)
+    for s, (info, t, tab) in zip(specs, host):
+        want = _alone(info, t, s.morton, s.solid)
+        assert torch.equal(tab, want), f"{s}: {int((tab != want).sum())} words differ from the request run alone"
+
+
+def test_server_admission_keeps_the_budget():
+    # 512^3 tables are 16 MiB each; a 40 MiB budget holds two such requests (with records) at a time.
+    specs = [meshgen.MeshSpec("torus", 20 + i, 24, 512, bool(i % 3 == 0), bool(i % 2)) for i in range(8)]
+    host = [_host(s) for s in specs]
+    budget = 40 << 20
+    with cv.Server(memory_budget_bytes=budget, max_batch=64, max_inflight=4) as srv:
+        ids = [srv.submit(info, t, tab, s.morton, s.solid) for s, (info, t, tab) in zip(specs, host)]
+        for i in ids:
+            srv.wait(i)
+        st = srv.stats()
+    assert st["memory_peak"] <= budget
+    assert st["batches"] >= 4, st  # memory, not max_batch, limited the batches
+    for s, (info, t, tab) in zip(specs, host):
+        assert torch.equal(tab, _alone(info, t, s.morton, s.solid)), s
+
+
+def test_server_refuses_a_request_larger_than_the_budget():
+    info, t, tab = _host(meshgen.MeshSpec("torus", 1, 16, 512, False, False))
+    with cv.Server(memory_budget_bytes=8 << 20, max_batch=4, max_inflight=1) as srv:
+        with pytest.raises(cv.CvxError) as e:
+            srv.submit(info, t, tab)
+        assert e.value.status == 3
+        assert srv.stats()["completed"] == 0
+
+
+def test_server_empty_mesh_returns_a_cleared_table():
+    tris = np.zeros((0, 9), dtype=np.float32)
+    info = cv.make_info((0, 0, 0), (1, 1, 1), 64, 0)
+    tab = torch.full((cv.table_words(info),), GARBAGE, dtype=torch.int32).pin_memory()
+    with cv.Server(memory_budget_bytes=16 << 20, max_batch=4, max_inflight=2) as srv:
+        srv.wait(srv.submit(info, torch.from_numpy(tris.reshape(-1)), tab, False, True))
+    assert int(tab.count_nonzero()) == 0
+
+
+def test_server_open_loop_replay():
+    specs = _mesh_requests(6, seed=5, max_tris=40_000)
+    host = [_host(s) for s in specs]
+    pool = [cv.Server.request(info, t, tab, s.morton, s.solid) for s, (info, t, tab) in zip(specs, host)]
+    arrivals = meshgen.poisson_arrivals(3000.0, 0.03, seed=1)
+    index = np.random.default_rng(2).integers(0, len(pool), size=len(arrivals))
+    with cv.Server(memory_budget_bytes=1 << 30, max_batch=16, max_inflight=2) as srv:
+        lat = srv.replay(pool, index, arrivals)
+        st = srv.stats()
+    assert len(lat) == len(arrivals) > 20 and np.all(lat > 0) and np.all(np.isfinite(lat))
+    assert st["completed"] == len(arrivals)
+    for s, (info, t, tab) in zip(specs, host):
+        if np.any(index == specs.index(s)):
+            assert torch.equal(tab, _alone(info, t, s.morton, s.solid)), s
