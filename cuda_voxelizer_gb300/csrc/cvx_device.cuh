@@ -219,18 +219,29 @@ __device__ __forceinline__ void or_span(uint32_t* table, uint64_t lo, uint64_t h
 	}
 }
 
+// Dilated-integer step of the x bits of a Morton code (x at bit positions 0, 3, 6, ...):
+// code(x + d) from code(x) for d = 1 (kMortonX1) or d = 4 (kMortonX4), without re-spreading x.
+constexpr uint64_t kMortonXMask = 0x249249249249ull;
+constexpr uint64_t kMortonX1 = 1ull, kMortonX4 = 64ull;
+__device__ __forceinline__ uint64_t morton_x_add(uint64_t xd, uint64_t step) {
+	return ((xd | ~kMortonXMask) + step) & kMortonXMask;
+}
+
 // OR the Morton-ordered bits of row (y, z), x in [xl, xh], one atomic per touched word.  Within a
 // Morton word (32 consecutive codes) x varies in its two low bits only: codes of x = 4k..4k+3 sit at
-// offsets {0, 1, 8, 9} from the code of x = 4k.
+// offsets {0, 1, 8, 9} from the code of x = 4k, i.e. MSB-first bits 31, 30, 23, 22 shifted right
+// by that code's offset in its word.
 __device__ __forceinline__ void or_span_morton(uint32_t* table, int xl, int xh, uint32_t y, uint32_t z) {
 	const uint64_t yz = (spread3(y) << 1) | (spread3(z) << 2);
-	for (int k = xl >> 2; k <= (xh >> 2); k++) {
-		uint64_t code = spread3((uint32_t)(k << 2)) | yz;
-		uint32_t base = (uint32_t)(code & 31u);
-		uint32_t m = 0;
-		int j0 = max(xl - (k << 2), 0), j1 = min(xh - (k << 2), 3);
-		for (int j = j0; j <= j1; j++) m |= 0x80000000u >> (base + (uint32_t)(j & 1) + 8u * (uint32_t)(j >> 1));
-		atomicOr(table + (code >> 5), m);
+	const int k1 = xh >> 2;
+	uint64_t xd = spread3((uint32_t)(xl & ~3));
+	for (int k = xl >> 2; k <= k1; k++) {
+		const uint64_t code = xd | yz;
+		const int j0 = max(xl - (k << 2), 0), j1 = min(xh - (k << 2), 3);
+		const uint32_t n = (0xFu << j0) & (0xFu >> (3 - j1));  // x offsets j0..j1 of the group
+		const uint32_t m = ((n & 1u) << 31) | ((n & 2u) << 29) | ((n & 4u) << 21) | ((n & 8u) << 19);
+		atomicOr(table + (code >> 5), m >> (uint32_t)(code & 31u));
+		xd = morton_x_add(xd, kMortonX4);
 	}
 }
 

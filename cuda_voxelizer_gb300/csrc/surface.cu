@@ -261,9 +261,10 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 			WordSink sink{table};
 			const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
 			const uint64_t yzm = morton ? ((spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2)) : 0;
+			uint64_t xd = morton ? spread3((uint32_t)S.bx0) : 0;
 			for (int x = S.bx0; x <= S.bx1; x++) {
-				if (!voxel_pass<P>(S, K, unit[0], x)) continue;
-				sink.add(morton ? (spread3((uint32_t)x) | yzm) : base + (uint64_t)x);
+				if (voxel_pass<P>(S, K, unit[0], x)) sink.add(morton ? (xd | yzm) : base + (uint64_t)x);
+				if (morton) xd = morton_x_add(xd, kMortonX1);
 			}
 			sink.flush();
 		} else {
