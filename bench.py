@@ -161,6 +161,33 @@ def traffic_from_profiles(kernel: str):
         return None
 
 
+def step_roofline(cv, torch, T, table_bytes, hbm_gbs, ms_per_step):
+    """Roofline of one step by bytes and atomics: per call t = max(B / BW, A / R_atom) with
+    B = 36 T + table (+ table again for the solid flip table) and A the exact atomic count of the
+    workload (profiles/atomic_terms.json, counted by the oracle); R_atom is the scattered 32-bit
+    atomicOr rate measured here on a 128 MiB table."""
+    from cuda_voxelizer_gb300 import _lib
+    try:
+        with open(os.path.join(ROOT, "profiles", "atomic_terms.json")) as f:
+            terms = json.load(f)["icosphere_l8_512"]
+    except Exception:
+        return None
+    words = 32 << 20
+    buf = torch.zeros(words, dtype=torch.int32, device="cuda")
+    r_atom = max(_lib.lib.cvx_microbench_atomic_or(buf.data_ptr(), words, 0, 152 * 8, 64) for _ in range(3))
+    del buf
+    calls, t_roof = {}, 0.0
+    for (morton, solid), name in zip(MODES, ("surface_linear", "surface_morton", "solid_linear", "solid_morton")):
+        b = 36 * T + table_bytes * (2 if solid else 1)
+        a = int(terms[name])
+        tb, ta = b / (hbm_gbs * 1e9), a / r_atom
+        calls[name] = {"bytes": b, "atomics": a, "t_bytes_us": tb * 1e6, "t_atomics_us": ta * 1e6}
+        t_roof += max(tb, ta)
+    return {"definition": "sum over the 4 calls of max(B/BW_hbm, A/R_atom)", "r_atom_per_s": r_atom,
+            "hbm_gbs": hbm_gbs, "calls": calls, "t_roof_us": t_roof * 1e6, "t_measured_us": ms_per_step * 1e3,
+            "frac": t_roof / (ms_per_step / 1e3)}
+
+
 def cpu_sample(tris):
     n = tris.shape[0] // SAMPLE_FRACTION
     return np.ascontiguousarray(tris[:n])
@@ -301,7 +328,8 @@ def main():
     traffic = traffic_from_profiles(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                "kernel_ms_per_step": kernel_ms, "alg_bytes_per_launch": alg.get(dom, 0)}
+                "kernel_ms_per_step": kernel_ms, "alg_bytes_per_launch": alg.get(dom, 0),
+                "step": step_roofline(cv, torch, T, table_bytes, peak, ms)}
 
     # ---- end to end through the public API with host buffers -------------------------------------
     h_tris = torch.from_numpy(tris.reshape(-1)).pin_memory()

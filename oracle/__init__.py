@@ -53,6 +53,8 @@ def lib():
         L.ovx_info_init.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_uint64]
         L.ovx_max_threads.restype = ctypes.c_int
+        L.ovx_count_atomics.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.ovx_count_atomics.restype = ctypes.c_uint64
         _lib = L
     return _lib
 
@@ -102,6 +104,14 @@ def voxelize_omp(info: bytes, tris, morton: bool = False, solid: bool = False, t
     table = np.zeros(table_words(info), dtype=np.uint32)
     lib().ovx_voxelize_omp(ctypes.addressof(ib), _ptr(t), _ptr(table), int(morton), int(solid), int(threads))
     return table
+
+
+def count_atomics(info: bytes, tris, morton: bool = False, solid: bool = False) -> int:
+    """Atomic term of the roofline: distinct table words per triangle summed (surface) or column
+    hits (solid), counted by the restatement without writing a table."""
+    t = _soup(tris, info)
+    ib = ctypes.create_string_buffer(bytes(info), 64)
+    return int(lib().ovx_count_atomics(ctypes.addressof(ib), _ptr(t), int(morton), int(solid)))
 
 
 def max_threads() -> int:

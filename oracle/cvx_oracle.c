@@ -157,9 +157,31 @@ void ovx_morton_lut(int axis, uint32_t out[256]) {
 
 static int g_parallel = 0;
 
+/* Counting pass (ovx_count_atomics, serial only): surface bit writes record their word instead of
+ * writing it; solid column hits are counted before their bits are written. */
+static int g_count = 0;
+static uint64_t* g_words = NULL;
+static size_t g_nwords = 0, g_capwords = 0;
+static uint64_t g_hits = 0;
+
+static void count_word(uint64_t w) {
+    if (g_nwords == g_capwords) {
+        size_t cap = g_capwords ? 2 * g_capwords : 4096;
+        uint64_t* p = (uint64_t*)realloc(g_words, cap * sizeof(uint64_t));
+        if (!p) abort();
+        g_words = p;
+        g_capwords = cap;
+    }
+    g_words[g_nwords++] = w;
+}
+
 static inline void set_bit(uint32_t* table, uint64_t index) {
     uint64_t w = index / 32u;
     uint32_t mask = 1u << (31u - (uint32_t)(index % 32u));
+    if (g_count) {
+        count_word(w);
+        return;
+    }
     if (g_parallel) {
 #ifdef _OPENMP
 #pragma omp critical
@@ -341,6 +363,10 @@ static void solid_triangle(const ovx_info* info, const float* tri, uint64_t t, u
                  * kernel keeps it signed (src/voxelize_solid.cu:123-124).  They only differ for
                  * hits left of the grid, where the CPU loop runs away; both stop here. */
                 if (xmax < 0) continue;
+                if (g_count) {
+                    g_hits++;
+                    continue;
+                }
                 for (int64_t x = 0; x <= xmax; x++) {
                     uint64_t loc;
                     if (morton) {
@@ -374,6 +400,39 @@ void ovx_voxelize(const ovx_info* info, const float* tris, uint32_t* table, int 
         if (solid) solid_triangle(info, tris + 9 * t, t, table, words, morton, mode);
         else surface_triangle(info, tris + 9 * t, t, table, morton, mode);
     }
+}
+
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : (x > y);
+}
+
+/* The atomic term of the roofline, counted exactly from the mesh: surface, the number of distinct
+ * table words each triangle sets a bit in, summed over triangles; solid, the number of column hits
+ * (every hit flips a run of bits in one row).  Serial; the table is not written. */
+uint64_t ovx_count_atomics(const ovx_info* info, const float* tris, int morton, int solid) {
+    init_luts();
+    g_parallel = 0;
+    g_count = 1;
+    g_hits = 0;
+    uint64_t total = 0, words = words_for(info);
+    for (uint64_t t = 0; t < info->n_tri; t++) {
+        if (solid) {
+            solid_triangle(info, tris + 9 * t, t, NULL, words, morton, NULL);
+            continue;
+        }
+        g_nwords = 0;
+        surface_triangle(info, tris + 9 * t, t, NULL, morton, NULL);
+        if (g_nwords > 1) qsort(g_words, g_nwords, sizeof(uint64_t), cmp_u64);
+        for (size_t i = 0; i < g_nwords; i++)
+            if (i == 0 || g_words[i] != g_words[i - 1]) total++;
+    }
+    if (solid) total = g_hits;
+    g_count = 0;
+    free(g_words);
+    g_words = NULL;
+    g_nwords = g_capwords = 0;
+    return total;
 }
 
 /* The same restatement run the way the reference runs it on the host: an OpenMP parallel for

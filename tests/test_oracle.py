@@ -114,3 +114,25 @@ def test_oracle_matches_reference_live(seed):
             a = oracle.voxelize(bytes(raw), t, morton=morton, solid=solid)
             b = oracle.ref_cpu_voxelize(bytes(raw), t, morton=morton, solid=solid)
             assert np.array_equal(a, b), (g, morton, solid)
+
+
+@pytest.mark.parametrize("solid", [False, True])
+@pytest.mark.parametrize("morton", [False, True])
+def test_count_atomics_matches_per_triangle_tables(morton, solid):
+    """The roofline's atomic term: one triangle at a time, the surface count is the number of
+    nonzero table words and the solid count the number of rows it flips (one hit per column)."""
+    from cuda_voxelizer_gb300 import meshgen
+    tris = meshgen.torus(3, nu=12, nv=6)
+    info = oracle.info_init(*oracle.mesh_bbcube(tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)), (32, 32, 32),
+                            tris.shape[0])
+    want = 0
+    for t in tris:
+        one = oracle.with_count(info, 1)
+        tab = oracle.voxelize(one, t.reshape(1, 9), morton=morton, solid=solid)
+        if not solid:
+            want += int(np.count_nonzero(tab))
+        else:
+            lin = tab if not morton else oracle.voxelize(one, t.reshape(1, 9), solid=True)
+            bits = np.unpackbits(lin.view(np.uint8).reshape(-1, 4)[:, ::-1].reshape(-1)).reshape(32 * 32, 32)
+            want += int(np.count_nonzero(bits.any(axis=1)))
+    assert oracle.count_atomics(info, tris, morton=morton, solid=solid) == want
