@@ -384,7 +384,8 @@ def main():
             specs = meshgen.batch_mix(0, 256)
             mix = [(s, s.build()) for s in specs]
             extras.update(bench_batch(cv, torch, mix))
-            extras.update(bench_serve(cv, meshgen, torch, mix, args.serve_seconds))
+            extras.update(bench_serve(cv, meshgen, torch, mix, args.serve_seconds,
+                                      extras["batch_256"]["plan_meshes_s"]))
         line["extras"] = extras
         print(json.dumps(line), flush=True)
 
@@ -484,47 +485,101 @@ def bench_batch(cv, torch, mix):
                           "speedup_vs_plain": plain_s / plan_s}}
 
 
-def bench_serve(cv, meshgen, torch, mix, seconds):
-    """Open-loop serving of the 256-mesh distribution: Poisson arrivals, 40 GiB budget, host buffers
-    in and out.  Capacity is measured with a burst (every request due at t=0); the Poisson sweep then
-    runs at fractions of it.  The plain arm is the same server limited to one request at a time on
-    one stream, i.e. one synchronous per-request launch after another."""
-    pool, keep = [], []
+def copy_rates(torch, nbytes=1 << 30):
+    """Pinned host<->device copy rates (bytes/s): each direction alone and both at once."""
+    h1 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d1 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    def both():
+        with torch.cuda.stream(s1):
+            d1.copy_(h1, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    h2d = nbytes / timed(lambda: d1.copy_(h1, non_blocking=True))
+    d2h = nbytes / timed(lambda: h2.copy_(d2, non_blocking=True))
+    duplex = 2 * nbytes / timed(both)
+    return {"h2d_gbs": h2d / 1e9, "d2h_gbs": d2h / 1e9, "both_directions_gbs": duplex / 1e9}
+
+
+def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
+    """Open-loop serving of the 256-mesh distribution: Poisson arrivals, 40 GiB budget.  Two request
+    kinds: host buffers (pinned triangles copied in, the table copied out) and device-resident
+    buffers (triangles uploaded once, the table kept on the device; replay releases it at
+    completion).  Capacity is measured with a burst (every request due at t=0); the Poisson sweep
+    then runs at fractions of it.  The plain arm is the same server limited to one request at a
+    time on one stream: one per-request launch sequence after another."""
+    host_pool, dev_pool, keep = [], [], []
+    in_bytes = out_bytes = 0
     for s, t in mix:
         info = cv.make_voxinfo(t, s.gridsize)
         h_t = torch.from_numpy(t.reshape(-1)).pin_memory()
         h_tab = torch.empty(cv.table_words(info), dtype=torch.int32).pin_memory()
-        keep.append((h_t, h_tab))
-        pool.append(cv.Server.request(info, h_t, h_tab, s.morton, s.solid))
+        d_t = h_t.cuda()
+        keep.append((h_t, h_tab, d_t))
+        host_pool.append(cv.Server.request(info, h_t, h_tab, s.morton, s.solid))
+        dev_pool.append(cv.Server.request(info, d_t, None, s.morton, s.solid))
+        in_bytes += t.nbytes
+        out_bytes += 4 * cv.table_words(info)
+    torch.cuda.synchronize()
     rng = np.random.default_rng(7)
 
-    def burst(srv, n):
+    def burst(srv, pool, n):
         lat = srv.replay(pool, rng.integers(0, len(pool), n), np.zeros(n))
         return n / (float(lat.max()) / 1e3)
 
-    def poisson(srv, rate, seed):
+    def poisson(srv, pool, rate, seed):
         arr = meshgen.poisson_arrivals(rate, seconds, seed=seed)
         lat = srv.replay(pool, rng.integers(0, len(pool), len(arr)), arr)
         span = float(np.max(arr + lat / 1e3))
         return {"rate_per_s": round(rate, 1), "requests": int(len(arr)), "meshes_s": len(arr) / span,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
 
+    def arm(pool, max_batch, max_inflight, fracs, seed0, n_burst):
+        mk = lambda: cv.Server(memory_budget_bytes=40 << 30, max_batch=max_batch, max_inflight=max_inflight)
+        with mk() as srv:
+            burst(srv, pool, max(64, n_burst // 8))
+        with mk() as srv:
+            cap = burst(srv, pool, n_burst)
+            st = srv.stats()
+        res = {"capacity_meshes_s": cap, "max_batch": max_batch, "max_inflight": max_inflight,
+               "burst_requests": n_burst, "burst_mean_batch": st["mean_batch"],
+               "burst_memory_peak_gib": st["memory_peak"] / 2 ** 30}
+        with mk() as srv:
+            res["sweep"] = [poisson(srv, pool, f * cap, seed0 + i) for i, f in enumerate(fracs)]
+        return res
+
+    rates = copy_rates(torch)
+    n = len(mix)
+    per_req_in, per_req_out = in_bytes / n, out_bytes / n
+    copy_cap = 1.0 / max(per_req_in / (rates["h2d_gbs"] * 1e9), per_req_out / (rates["d2h_gbs"] * 1e9),
+                         (per_req_in + per_req_out) / (rates["both_directions_gbs"] * 1e9))
     out = {"budget_gib": 40, "seconds_per_rate": seconds, "pool": "256-mesh mix (same as batch_256)",
-           "host_buffers": "pinned, triangles in and table out per request"}
-    with cv.Server(memory_budget_bytes=40 << 30, max_batch=256, max_inflight=4) as srv:
-        burst(srv, 512)
-        cap = burst(srv, 4096)
-        out["served"] = {"capacity_meshes_s": cap, "max_batch": 256, "max_inflight": 4,
-                         "sweep": [poisson(srv, f * cap, i) for i, f in enumerate((0.25, 0.5, 0.75, 0.9))]}
-        st = srv.stats()
-        out["served"]["mean_batch"] = st["mean_batch"]
-        out["served"]["memory_peak_gib"] = st["memory_peak"] / 2 ** 30
-    with cv.Server(memory_budget_bytes=40 << 30, max_batch=1, max_inflight=1) as srv:
-        burst(srv, 64)
-        pcap = burst(srv, 512)
-        out["plain"] = {"capacity_meshes_s": pcap,
-                        "sweep": [poisson(srv, f * pcap, 10 + i) for i, f in enumerate((0.5, 0.9))]}
-    out["served_vs_plain_capacity"] = cap / pcap
+           "copy_rates": rates, "bytes_per_request": {"in": per_req_in, "out": per_req_out}}
+    fr = (0.25, 0.5, 0.75, 0.9)
+    host = {"served": arm(host_pool, 16, 16, fr, 0, 4096), "plain": arm(host_pool, 1, 1, (0.5, 0.9), 10, 512)}
+    host["roofline_meshes_s"] = min(copy_cap, plan_meshes_s)
+    host["served_frac_of_roofline"] = host["served"]["capacity_meshes_s"] / host["roofline_meshes_s"]
+    host["served_vs_plain_capacity"] = host["served"]["capacity_meshes_s"] / host["plain"]["capacity_meshes_s"]
+    dev = {"served": arm(dev_pool, 256, 4, fr, 20, 8192), "plain": arm(dev_pool, 1, 1, (0.5, 0.9), 30, 1024)}
+    dev["roofline_meshes_s"] = plan_meshes_s
+    dev["served_frac_of_roofline"] = dev["served"]["capacity_meshes_s"] / plan_meshes_s
+    dev["served_vs_plain_capacity"] = dev["served"]["capacity_meshes_s"] / dev["plain"]["capacity_meshes_s"]
+    out["host_buffers"] = host
+    out["device_resident"] = dev
+    out["roofline_note"] = ("host buffers: min(copy-bound rate from the measured pinned copy rates, batched "
+                            "compute rate of batch_256); device-resident: the batched compute rate")
     return {"serve": out}
 
 

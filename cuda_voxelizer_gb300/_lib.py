@@ -38,8 +38,8 @@ class CvxServerConfig(ctypes.Structure):
 
 
 class CvxServerRequest(ctypes.Structure):
-    _fields_ = [("info", CvxVoxinfo), ("h_triangles", vp), ("h_table", vp), ("morton", ctypes.c_int32),
-                ("solid", ctypes.c_int32)]
+    _fields_ = [("info", CvxVoxinfo), ("h_triangles", vp), ("d_triangles", vp), ("h_table", vp),
+                ("morton", ctypes.c_int32), ("solid", ctypes.c_int32)]
 
 
 class CvxServerStats(ctypes.Structure):
@@ -76,6 +76,8 @@ SIGNATURES = {
     "cvx_server_create": (c_status, [ctypes.POINTER(CvxServerConfig), ctypes.POINTER(vp)]),
     "cvx_server_submit": (c_status, [vp, ctypes.POINTER(CvxServerRequest), ctypes.POINTER(u64)]),
     "cvx_server_wait": (c_status, [vp, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "cvx_server_table": (c_status, [vp, u64, ctypes.POINTER(vp)]),
+    "cvx_server_release": (c_status, [vp, u64]),
     "cvx_server_stats_get": (c_status, [vp, ctypes.POINTER(CvxServerStats)]),
     "cvx_server_replay": (c_status, [vp, ctypes.POINTER(CvxServerRequest), u32, ctypes.POINTER(ctypes.c_double),
                                      ctypes.POINTER(ctypes.c_double)]),

@@ -259,19 +259,38 @@ class Server:
 
     @staticmethod
     def request(info: VoxInfo, triangles, table, morton_code: bool = False, solid: bool = False) -> CvxServerRequest:
-        if _host_nbytes(triangles) < 36 * info.n_triangles:
-            raise ValueError("triangle buffer smaller than 9 floats per triangle")
-        if _host_nbytes(table) < 4 * table_words(info):
+        """``triangles``: a host buffer (copied in) or a CUDA tensor (read in place on the device).
+        ``table``: a host buffer the result is copied to, or None to keep the table resident on
+        the device (see :meth:`table` and :meth:`release`)."""
+        if hasattr(triangles, "is_cuda") and triangles.is_cuda:
+            _check_sizes(info, triangles, None)
+            h_t, d_t = None, _ptr(triangles)
+        else:
+            if _host_nbytes(triangles) < 36 * info.n_triangles:
+                raise ValueError("triangle buffer smaller than 9 floats per triangle")
+            h_t, d_t = _host_ptr(triangles, False), None
+        if table is not None and _host_nbytes(table) < 4 * table_words(info):
             raise ValueError(f"table buffer smaller than {4 * table_words(info)} bytes")
-        return CvxServerRequest(info, _host_ptr(triangles, False), _host_ptr(table, True), int(bool(morton_code)),
-                                int(bool(solid)))
+        h_tab = _host_ptr(table, True) if table is not None else None
+        return CvxServerRequest(info, h_t, d_t, h_tab, int(bool(morton_code)), int(bool(solid)))
 
-    def submit(self, info: VoxInfo, triangles, table, morton_code: bool = False, solid: bool = False) -> int:
+    def submit(self, info: VoxInfo, triangles, table=None, morton_code: bool = False, solid: bool = False) -> int:
         req = self.request(info, triangles, table, morton_code, solid)
         rid = ctypes.c_uint64()
         check(lib.cvx_server_submit(self._h, ctypes.byref(req), ctypes.byref(rid)), "cvx_server_submit")
         self._keep[rid.value] = (triangles, table)
         return rid.value
+
+    def table(self, rid: int) -> int:
+        """Device address of a completed request's resident table (valid until release)."""
+        p = ctypes.c_void_p()
+        check(lib.cvx_server_table(self._h, int(rid), ctypes.byref(p)), "cvx_server_table")
+        return int(p.value or 0)
+
+    def release(self, rid: int) -> None:
+        """Frees a completed request's resident table."""
+        check(lib.cvx_server_release(self._h, int(rid)), "cvx_server_release")
+        self._keep.pop(int(rid), None)
 
     def wait(self, rid: int, timeout_ms: float = -1.0) -> float:
         """Waits for request ``rid``; returns its latency in ms (submission to table written)."""

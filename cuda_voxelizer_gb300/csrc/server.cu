@@ -13,6 +13,9 @@
 // Memory.  All device memory of a request -- triangles, table, solid flip table -- and its batch's
 // work records come from one arena of the budget's size, allocated when the server is created and
 // carved first-fit, so nothing is allocated while serving and the budget is a hard limit.
+// Requests may keep their buffers on the device: triangles already resident (d_triangles, read in
+// place) and the table left resident in the arena (no host table) until cvx_server_release, for
+// consumers that use it on the GPU.
 // Admission is strictly in arrival order: a request that does not fit waits (and so do the ones
 // behind it) until batches finish.  A request larger than the whole budget is refused at submission.
 #include <cuda_runtime.h>
@@ -106,7 +109,11 @@ private:
 struct Request {
 	uint64_t id = 0;
 	cvx_server_request req{};
-	size_t tri_bytes = 0, table_bytes = 0, flip_bytes = 0;
+	bool device_tris = false;     // triangles read in place from req.d_triangles
+	bool resident_table = false;  // no host table and kept: the table stays in the arena until released
+	bool copy_out = true;         // the table is copied to req.h_table
+	bool waited = false;
+	size_t tri_bytes = 0, table_bytes = 0, flip_bytes = 0;  // arena bytes (tri_bytes 0 for device_tris)
 	void* d_tris = nullptr;
 	void* d_table = nullptr;
 	void* d_flips = nullptr;
@@ -180,16 +187,21 @@ struct cvx_server {
 		return true;
 	}
 	void unadmit(Request& r) {
-		arena.release(r.d_tris);
+		release_work(r);
 		arena.release(r.d_table);
+		r.d_table = nullptr;
+	}
+	// The memory a request needs only while its batch runs (its table may stay resident).
+	void release_work(Request& r) {
+		arena.release(r.d_tris);
 		arena.release(r.d_flips);
-		r.d_tris = r.d_table = r.d_flips = nullptr;
+		r.d_tris = r.d_flips = nullptr;
 	}
 
 	static cvx_job job_of(const Request& r) {
 		cvx_job j{};
 		j.info = r.req.info;
-		j.d_triangles = static_cast<const float*>(r.d_tris);
+		j.d_triangles = r.device_tris ? r.req.d_triangles : static_cast<const float*>(r.d_tris);
 		j.d_table = static_cast<uint32_t*>(r.d_table);
 		j.morton = r.req.morton;
 		j.solid = r.req.solid;
@@ -265,7 +277,7 @@ struct cvx_server {
 		std::vector<uint32_t*> flips;
 		for (auto& r : sl.reqs) {
 			if (!ok) break;
-			if (r->tri_bytes)
+			if (r->tri_bytes)  // host triangles (device triangles are read in place)
 				ok = cuda_ok(cudaMemcpyAsync(r->d_tris, r->req.h_triangles, r->tri_bytes, cudaMemcpyHostToDevice, st),
 				             "cudaMemcpyAsync(triangles)");
 			const uint64_t words = r->table_bytes / 4;
@@ -293,6 +305,7 @@ struct cvx_server {
 		}
 		for (auto& r : sl.reqs) {
 			if (!ok) break;
+			if (!r->copy_out) continue;
 			ok = cuda_ok(cudaMemcpyAsync(r->req.h_table, r->d_table, r->table_bytes, cudaMemcpyDeviceToHost, st),
 			             "cudaMemcpyAsync(table)");
 		}
@@ -310,7 +323,8 @@ struct cvx_server {
 		for (auto& r : sl.reqs) {
 			r->latency_ms = std::chrono::duration<double, std::milli>(sl.finish_time - r->arrival).count();
 			r->done = true;
-			unadmit(*r);
+			if (r->resident_table) release_work(*r);
+			else unadmit(*r);
 			latencies.push_back(r->latency_ms);
 			completed++;
 		}
@@ -353,7 +367,10 @@ struct cvx_server {
 		}
 	}
 
-	cvx_status submit(const cvx_server_request* q, Clock::time_point arrival, uint64_t* out_id) {
+	// discard_table: a request without a host table whose table nobody will read (the replay load
+	// generator) is freed at completion instead of staying resident.
+	cvx_status submit(const cvx_server_request* q, Clock::time_point arrival, uint64_t* out_id,
+	                  bool discard_table = false) {
 		if (!q || !out_id) {
 			cvx::set_message("cvx_server_submit: null argument");
 			return CVX_ERR_INVALID_VALUE;
@@ -365,8 +382,8 @@ struct cvx_server {
 				return CVX_ERR_INVALID_VALUE;
 			}
 		}
-		if ((v.n_triangles && !q->h_triangles) || !q->h_table) {
-			cvx::set_message("cvx_server_submit: null host buffer");
+		if (v.n_triangles && !q->h_triangles && !q->d_triangles) {
+			cvx::set_message("cvx_server_submit: no triangles (host or device)");
 			return CVX_ERR_INVALID_VALUE;
 		}
 		if (q->morton) {
@@ -378,7 +395,10 @@ struct cvx_server {
 		}
 		auto r = std::make_shared<Request>();
 		r->req = *q;
-		r->tri_bytes = (size_t)v.n_triangles * 9 * sizeof(float);
+		r->device_tris = q->d_triangles != nullptr;
+		r->copy_out = q->h_table != nullptr;
+		r->resident_table = !r->copy_out && !discard_table;
+		r->tri_bytes = r->device_tris ? 0 : (size_t)v.n_triangles * 9 * sizeof(float);
 		r->table_bytes = (size_t)cvx_table_words(&v) * 4;
 		r->flip_bytes = q->solid ? r->table_bytes : 0;
 		// Fits an empty budget? (its own memory plus the records of a batch holding it alone)
@@ -411,6 +431,31 @@ struct cvx_server {
 		return CVX_OK;
 	}
 
+	// A completed request's resident table: its device address, or its release.
+	cvx_status table(uint64_t id, uint32_t** d_table) {
+		std::lock_guard<std::mutex> lk(mu);
+		auto it = live.find(id);
+		if (it == live.end() || !it->second->resident_table || !it->second->done) {
+			cvx::set_message("cvx_server_table: no completed request with a resident table under this id");
+			return CVX_ERR_INVALID_VALUE;
+		}
+		*d_table = static_cast<uint32_t*>(it->second->d_table);
+		return CVX_OK;
+	}
+	cvx_status release(uint64_t id) {
+		std::lock_guard<std::mutex> lk(mu);
+		auto it = live.find(id);
+		if (it == live.end() || !it->second->resident_table || !it->second->done) {
+			cvx::set_message("cvx_server_release: no completed request with a resident table under this id");
+			return CVX_ERR_INVALID_VALUE;
+		}
+		arena.release(it->second->d_table);
+		it->second->d_table = nullptr;
+		live.erase(it);
+		cv_work.notify_one();  // memory came free: pending requests may fit now
+		return CVX_OK;
+	}
+
 	cvx_status wait(uint64_t id, double timeout_ms, double* latency_ms) {
 		std::unique_lock<std::mutex> lk(mu);
 		auto it = live.find(id);
@@ -426,7 +471,14 @@ struct cvx_server {
 			cvx::set_message("cvx_server_wait: timed out");
 			return CVX_ERR_INVALID_VALUE;
 		}
-		live.erase(id);
+		r->waited = true;
+		if (!r->resident_table || r->status != CVX_OK) {
+			if (r->resident_table) {
+				arena.release(r->d_table);
+				r->d_table = nullptr;
+			}
+			live.erase(id);
+		}
 		if (latency_ms) *latency_ms = r->latency_ms;
 		if (r->status != CVX_OK) cvx::set_message(r->message);
 		return r->status;
@@ -485,6 +537,22 @@ cvx_status cvx_server_wait(cvx_server* s, uint64_t id, double timeout_ms, double
 	return s->wait(id, timeout_ms, latency_ms);
 }
 
+cvx_status cvx_server_table(cvx_server* s, uint64_t id, uint32_t** d_table) {
+	if (!s || !d_table) {
+		cvx::set_message("cvx_server_table: null argument");
+		return CVX_ERR_INVALID_VALUE;
+	}
+	return s->table(id, d_table);
+}
+
+cvx_status cvx_server_release(cvx_server* s, uint64_t id) {
+	if (!s) {
+		cvx::set_message("cvx_server_release: server is null");
+		return CVX_ERR_INVALID_VALUE;
+	}
+	return s->release(id);
+}
+
 cvx_status cvx_server_stats_get(cvx_server* s, cvx_server_stats* out) {
 	if (!s || !out) {
 		cvx::set_message("cvx_server_stats_get: null argument");
@@ -533,7 +601,7 @@ cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint
 		if (due - Clock::now() > std::chrono::microseconds(300)) std::this_thread::sleep_until(due - std::chrono::microseconds(200));
 		while (Clock::now() < due) {
 		}
-		const cvx_status st = s->submit(&reqs[i], due, &ids[i]);
+		const cvx_status st = s->submit(&reqs[i], due, &ids[i], reqs[i].h_table == nullptr);
 		if (st != CVX_OK) {
 			for (uint32_t k = 0; k < i; k++) s->wait(ids[k], -1.0, nullptr);
 			return st;

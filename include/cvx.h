@@ -140,9 +140,10 @@ cvx_status cvx_plan_destroy(cvx_plan* plan);
  * work records, and max_inflight streams.  A worker thread launches pending requests as one
  * batch (at most max_batch requests, in arrival order, as many as the free budget holds) whenever
  * a stream is free, so requests that arrive while others run go into the next batch and overlap
- * with them.  Each request's triangles are copied in and its table copied out within its batch;
- * host buffers should be pinned (page-locked) for the copies to overlap.  Results are identical
- * to cvx_voxelize / cvx_voxelize_solid on the same request. */
+ * with them.  A request's host triangles are copied in and its table copied out within its batch
+ * (host buffers should be pinned for the copies to overlap); device-resident triangles are read in
+ * place and a request without a host table keeps its table resident on the device.  Results are
+ * identical to cvx_voxelize / cvx_voxelize_solid on the same request. */
 typedef struct cvx_server cvx_server;
 typedef struct cvx_server_config {
 	uint64_t memory_budget_bytes;
@@ -151,8 +152,11 @@ typedef struct cvx_server_config {
 } cvx_server_config;
 typedef struct cvx_server_request {
 	cvx_voxinfo info;
-	const float* h_triangles;  /* 9 floats per triangle; read until the request completes */
-	uint32_t* h_table;         /* cvx_table_words(&info) words, written by the time it completes */
+	const float* h_triangles;  /* host, 9 floats per triangle, copied in; read until completion */
+	const float* d_triangles;  /* or device-resident triangles, read in place (then h_ is ignored) */
+	uint32_t* h_table;         /* host table, cvx_table_words(&info) words, written by completion;
+	                            * NULL: the table stays resident in the server's budget after
+	                            * completion (cvx_server_table) until cvx_server_release */
 	int32_t morton;
 	int32_t solid;
 } cvx_server_request;
@@ -171,9 +175,15 @@ cvx_status cvx_server_submit(cvx_server* s, const cvx_server_request* req, uint6
 /* Waits for request `id` (timeout_ms < 0: no limit) and forgets it; returns its status.  A timeout
  * returns CVX_ERR_INVALID_VALUE and keeps the request. */
 cvx_status cvx_server_wait(cvx_server* s, uint64_t id, double timeout_ms, double* latency_ms);
+/* Device address of a completed request's resident table (valid until cvx_server_release). */
+cvx_status cvx_server_table(cvx_server* s, uint64_t id, uint32_t** d_table);
+/* Frees a completed request's resident table and forgets the request. */
+cvx_status cvx_server_release(cvx_server* s, uint64_t id);
 cvx_status cvx_server_stats_get(cvx_server* s, cvx_server_stats* out);
 /* Open-loop load: submits reqs[i] at arrival_s[i] seconds after the call starts (arrival_s
- * ascending), waits for all and writes each latency, counted from its scheduled arrival. */
+ * ascending), waits for all and writes each latency, counted from its scheduled arrival.
+ * Tables of requests without a host table are freed as the requests complete (nothing reads
+ * them), so a replay measures voxelization with device-resident output. */
 cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint32_t n, const double* arrival_s,
                              double* latency_ms);
 /* Finishes the queued requests, then frees everything. */

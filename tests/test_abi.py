@@ -114,5 +114,6 @@ def test_server_config_validation_answers_without_a_gpu():
 
 def test_server_request_struct_layout():
     R = _lib.CvxServerRequest
-    assert ctypes.sizeof(R) == 64 + 8 + 8 + 4 + 4
-    assert R.h_triangles.offset == 64 and R.h_table.offset == 72 and R.solid.offset == 84
+    assert ctypes.sizeof(R) == 64 + 8 + 8 + 8 + 4 + 4
+    assert R.h_triangles.offset == 64 and R.d_triangles.offset == 72 and R.h_table.offset == 80
+    assert R.solid.offset == 92

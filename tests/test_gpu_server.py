@@ -108,3 +108,41 @@ def test_server_open_loop_replay():
     for s, (info, t, tab) in zip(specs, host):
         if np.any(index == specs.index(s)):
             assert torch.equal(tab, _alone(info, t, s.morton, s.solid)), s
+
+
+def _read_device_words(ptr, words):
+    """Copy `words` uint32 from a raw device address into a host tensor (through the CUDA runtime
+    the library itself links)."""
+    import ctypes
+    rt = ctypes.CDLL("libcudart.so.13")
+    out = torch.empty(words, dtype=torch.int32)
+    rc = rt.cudaMemcpy(ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ptr), ctypes.c_size_t(4 * words),
+                       ctypes.c_int(2))  # cudaMemcpyDeviceToHost
+    assert rc == 0
+    return out
+
+
+def test_server_device_resident_requests():
+    """Triangles already on the device are read in place; a request without a host table keeps
+    its table resident (inside the budget) until it is released."""
+    specs = _mesh_requests(12, seed=8, max_tris=50_000)
+    budget = 512 << 20
+    with cv.Server(memory_budget_bytes=budget, max_batch=8, max_inflight=2) as srv:
+        meshes = []
+        for s in specs:
+            tris = s.build()
+            meshes.append((s, cv.make_voxinfo(tris, s.gridsize), torch.from_numpy(tris.reshape(-1)).cuda()))
+        torch.cuda.synchronize()  # the server's streams do not order after torch's
+        reqs = [(s, info, d, srv.submit(info, d, None, s.morton, s.solid)) for s, info, d in meshes]
+        for s, info, d, rid in reqs:
+            srv.wait(rid)
+        used = srv.stats()["memory_used"]
+        assert used >= sum(4 * cv.table_words(info) for _, info, _, _ in reqs)  # tables still held
+        for s, info, d, rid in reqs:
+            got = _read_device_words(srv.table(rid), cv.table_words(info))
+            want = _alone(info, d.cpu(), s.morton, s.solid)
+            assert torch.equal(got, want), s
+            srv.release(rid)
+        assert srv.stats()["memory_used"] == 0
+        with pytest.raises(cv.CvxError):
+            srv.table(reqs[0][3])  # released
