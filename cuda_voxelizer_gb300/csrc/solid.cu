@@ -10,12 +10,17 @@
 // any set of [0, xmax] ranges is exactly what this produces.
 //
 // Kernels, in launch order:
-//   solid_classify  one CTA per 256-triangle tile (TMA bulk staging as in surface.cu); triangles
-//                   with at most `small_cols` columns are finished in the thread, others queued.
-//   solid_cols      persistent; each warp takes an item of up to kColsPerItem columns.
-//   solid_resolve   one warp per resolve unit (whole rows): segmented prefix XOR along x.
-//   solid_morton    Morton jobs only: gathers resolved linear bits into Morton words.
-//   solid_zero      Morton jobs only: clears the flip table (the transcode reads it shared).
+//   solid_classify      one CTA per 256-triangle tile (TMA bulk staging as in surface.cu); the
+//                       columns of triangles with at most `small_cols` columns are dealt over the
+//                       CTA, the other triangles queued.
+//   solid_cols          persistent; each warp takes items of up to kColsPerItem columns.
+//   solid_resolve       one thread per row run (whole rows; 16-byte words where rows are aligned):
+//                       prefix XOR along x, XORed into the linear table, flip table cleared.
+//   solid_morton_slab   Morton jobs with 32 <= g <= 1024: a CTA resolves a 16 x 16-row slab in
+//                       shared memory and writes it as 16^3 Morton blocks (128 contiguous words).
+//   solid_morton_brick  Morton jobs with g > 1024: groups of x-adjacent 32^3 bricks.
+//   solid_morton_small  Morton jobs with g < 32 (one word at a time), then solid_zero clears the
+//                       flip table.
 #include "engine.h"
 
 namespace cvx {
