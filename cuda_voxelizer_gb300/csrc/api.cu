@@ -679,6 +679,7 @@ struct cvx_plan {
 	cudaGraphExec_t exec = nullptr;
 	cudaGraph_t graph = nullptr;
 	void* rec = nullptr;
+	void* rec_solid = nullptr;     // counters and queues of the solid chain (runs beside the surface chain)
 	uint32_t* flips = nullptr;
 	JobDesc* staging = nullptr;
 	ClearRange* clears = nullptr;  // the tables the graph zeroes (CVX_PLAN_CLEAR_TABLES)
@@ -708,10 +709,16 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 	};
 	uint64_t flip_total = 0;
 	for (const JobDesc& j : solid) flip_total += flip_bytes_of(j);
-	const uint64_t cap = queue_cap(surf, solid);
+	const uint64_t cap = queue_cap(surf, {});
+	const uint64_t cap_solid = queue_cap({}, solid);
 	const size_t slots = job_slots(surf, solid);
 	const RecLayout lay = rec_layout(cap, slots);
+	const RecLayout lay_solid = rec_layout(cap_solid, 0);
 	if (cudaMalloc(&p->rec, lay.end) != cudaSuccess) {
+		cudaGetLastError();
+		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
+	}
+	if (!solid.empty() && cudaMalloc(&p->rec_solid, lay_solid.end) != cudaSuccess) {
 		cudaGetLastError();
 		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
 	}
@@ -742,8 +749,21 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 				return bail(cuda_fail(cudaGetLastError(), "clear list upload"));
 		}
 	}
-	cudaStream_t cs;
+	cudaStream_t cs, cs2;
+	cudaEvent_t fork_ev, join_ev;
 	if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "stream"));
+	if (cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking) != cudaSuccess) {
+		cudaStreamDestroy(cs);
+		return bail(cuda_fail(cudaGetLastError(), "stream"));
+	}
+	cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming);
+	cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming);
+	auto drop_streams = [&]() {
+		cudaStreamDestroy(cs);
+		cudaStreamDestroy(cs2);
+		cudaEventDestroy(fork_ev);
+		cudaEventDestroy(join_ev);
+	};
 	// Upload the job arrays once, outside the graph (the graph only reads them), in the order the
 	// capture below consumes them.
 	{
@@ -765,12 +785,12 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 			s2 = upload(rg);
 		}
 		if (s2 != CVX_OK) {
-			cudaStreamDestroy(cs);
+			drop_streams();
 			return bail(s2);
 		}
 	}
 	if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-		cudaStreamDestroy(cs);
+		drop_streams();
 		return bail(cuda_fail(cudaGetLastError(), "begin capture"));
 	}
 	cvx_status cst = CVX_OK;
@@ -778,9 +798,19 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		cst = cuda_fail(cudaGetLastError(), "table clear");
 	if (cst == CVX_OK && cudaMemsetAsync(p->rec, 0, sizeof(Counters), cs) != cudaSuccess)
 		cst = cuda_fail(cudaGetLastError(), "counter clear");
+	// The solid chain runs on a second captured stream with its own counters and queues, so the
+	// graph lets it overlap the surface chain (they touch different tables).
+	const bool fork = cst == CVX_OK && !solid.empty() && !surf.empty();
+	cudaStream_t ss = fork ? cs2 : cs;
+	if (fork && (cudaEventRecord(fork_ev, cs) != cudaSuccess || cudaStreamWaitEvent(cs2, fork_ev, 0) != cudaSuccess))
+		cst = cuda_fail(cudaGetLastError(), "capture fork");
+	if (cst == CVX_OK && p->rec_solid && cudaMemsetAsync(p->rec_solid, 0, sizeof(Counters), ss) != cudaSuccess)
+		cst = cuda_fail(cudaGetLastError(), "counter clear");
 	if (cst == CVX_OK) {
 		// Launch exactly like Runner::run, but with the job arrays already resident.
 		size_t used = 0;
+		void* rec_now = p->rec;
+		uint64_t cap_now = cap;
 		auto prep = [&](Group& g, LaunchDesc& L) {
 			std::memset(&L, 0, sizeof(L));
 			L.n_jobs = (uint32_t)g.jobs.size();
@@ -790,11 +820,11 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 			L.n_mbricks = g.mbricks;
 			L.n_mslabs = g.mslabs;
 			L.slab_smem = g.slab_smem;
-			L.scr.ctr = reinterpret_cast<Counters*>(p->rec);
-			const RecLayout l0 = rec_layout(cap, 0);
-			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(p->rec) + l0.big);
-			L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(p->rec) + l0.mid);
-			L.scr.cap = (uint32_t)cap;
+			L.scr.ctr = reinterpret_cast<Counters*>(rec_now);
+			const RecLayout l0 = rec_layout(cap_now, 0);
+			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(rec_now) + l0.big);
+			L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(rec_now) + l0.mid);
+			L.scr.cap = (uint32_t)cap_now;
 			if (g.jobs.size() == 1) {
 				L.single = g.jobs[0];
 			} else {
@@ -812,11 +842,13 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 			}
 		}
 		if (cst == CVX_OK && !solid.empty()) {
+			rec_now = p->rec_solid;
+			cap_now = cap_solid;
 			for (Group& g : make_groups(solid, true)) {
 				LaunchDesc L;
 				prep(g, L);
-				if (cudaMemsetAsync(p->rec, 0, kCountersResetBytes, cs) != cudaSuccess ||
-				    launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidToggles, nullptr) != cudaSuccess) {
+				if (cudaMemsetAsync(p->rec_solid, 0, kCountersResetBytes, ss) != cudaSuccess ||
+				    launch_solid(L, dev.tune, dev.cols_grid, ss, kSolidToggles, nullptr) != cudaSuccess) {
 					cst = cuda_fail(cudaGetLastError(), "capture solid");
 					break;
 				}
@@ -825,14 +857,17 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 				Group rg = resolve_group(solid);
 				LaunchDesc L;
 				prep(rg, L);
-				if (launch_solid(L, dev.tune, dev.cols_grid, cs, kSolidResolve, nullptr) != cudaSuccess)
+				if (launch_solid(L, dev.tune, dev.cols_grid, ss, kSolidResolve, nullptr) != cudaSuccess)
 					cst = cuda_fail(cudaGetLastError(), "capture resolve");
 			}
 		}
 	}
+	if (fork && (cudaEventRecord(join_ev, cs2) != cudaSuccess || cudaStreamWaitEvent(cs, join_ev, 0) != cudaSuccess) &&
+	    cst == CVX_OK)
+		cst = cuda_fail(cudaGetLastError(), "capture join");
 	cudaGraph_t graph = nullptr;
 	cudaError_t ee = cudaStreamEndCapture(cs, &graph);
-	cudaStreamDestroy(cs);
+	drop_streams();
 	if (cst != CVX_OK) {
 		if (graph) cudaGraphDestroy(graph);
 		return bail(cst);
@@ -855,6 +890,7 @@ cvx_status cvx_plan_destroy(cvx_plan* p) {
 	if (p->exec) cudaGraphExecDestroy(p->exec);
 	if (p->graph) cudaGraphDestroy(p->graph);
 	if (p->rec) cudaFree(p->rec);
+	if (p->rec_solid) cudaFree(p->rec_solid);
 	if (p->flips) cudaFree(p->flips);
 	if (p->staging) cudaFreeHost(p->staging);
 	if (p->clears) cudaFree(p->clears);
