@@ -418,6 +418,23 @@ def bench_soup(cv, meshgen, torch, stream, flush):
     eng_ms = float(np.median(ts))
     out["soup_1024"] = {"triangles": 2_000_000, "engine_ms": eng_ms, "engine_mtris_s": 2.0 / (eng_ms / 1e3),
                         "ref_cuda": "timed by --impl reference (extras.soup_1024_ref_cuda)"}
+    # roofline of the call: max(B / BW, A / R_atom), A from profiles/atomic_terms.json
+    try:
+        from cuda_voxelizer_gb300 import _lib
+        with open(os.path.join(ROOT, "profiles", "atomic_terms.json")) as f:
+            a = int(json.load(f)["soup_2m_1024"]["surface_linear"])
+        words = 32 << 20
+        buf = torch.zeros(words, dtype=torch.int32, device="cuda")
+        r_atom = max(_lib.lib.cvx_microbench_atomic_or(buf.data_ptr(), words, 0, 152 * 8, 64) for _ in range(3))
+        del buf
+        b = 36 * 2_000_000 + 4 * cv.table_words(info)
+        hbm, _ = peaks()
+        t_roof = max(b / (hbm * 1e9), a / r_atom)
+        out["soup_1024"]["roofline"] = {"bytes": b, "atomics": a, "r_atom_per_s": r_atom,
+                                        "t_bytes_ms": b / (hbm * 1e9) * 1e3, "t_atomics_ms": a / r_atom * 1e3,
+                                        "frac": t_roof / (eng_ms / 1e3)}
+    except Exception as e:
+        out["soup_1024"]["roofline"] = f"unavailable: {e}"
     return out
 
 

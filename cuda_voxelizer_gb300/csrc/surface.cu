@@ -370,15 +370,30 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 			const int incl_s = __shfl_sync(FULL, incl, s);
 			const int cnt_s = __shfl_sync(FULL, cnt, s);
 			const int ya_s = __shfl_sync(FULL, ya, s);
+			int y = 0, z = 0, xl = 0, xh = -1;
 			if (k < R) {
-				const int y = ya_s + (k - (incl_s - cnt_s));
-				const int z = z0 + s;
+				y = ya_s + (k - (incl_s - cnt_s));
+				z = z0 + s;
 				const float py = __fmul_rn(__int2float_rn(y), unit[1]);
 				const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
 				RowK K;
 				row_consts<P>(S, py, pz, K);
-				int xl, xh;
-				if (row_interval<P>(S, D, K, unit[0], xl, xh)) write_row(table, morton, grid, y, z, xl, xh);
+				if (!row_interval<P>(S, D, K, unit[0], xl, xh)) xh = -1;
+			}
+			// Short rows are written by their own lane.  Long rows are written by the whole warp, one
+			// row at a time with the lanes on consecutive words (linear) or x groups (Morton): a
+			// scattered atomic costs an L2 transaction of its own, a warp's atomics on one row
+			// share a few lines.
+			const bool has = xh >= xl;
+			const bool wide = has && (morton ? (xh >> 2) - (xl >> 2) >= 4 : (xh >> 5) - (xl >> 5) >= 2);
+			if (has && !wide) write_row(table, morton, grid, y, z, xl, xh);
+			uint32_t todo = __ballot_sync(FULL, wide);
+			while (todo) {
+				const int src = __ffs(todo) - 1;
+				todo &= todo - 1u;
+				const int ry = __shfl_sync(FULL, y, src), rz = __shfl_sync(FULL, z, src);
+				const int rl = __shfl_sync(FULL, xl, src), rh = __shfl_sync(FULL, xh, src);
+				write_row_warp(table, morton, grid, ry, rz, rl, rh, lane);
 			}
 		}
 	}

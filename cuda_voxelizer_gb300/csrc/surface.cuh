@@ -351,4 +351,29 @@ __device__ __forceinline__ void write_row(uint32_t* table, bool morton, const ui
 	}
 }
 
+// write_row by a whole warp (every lane calls it with the same row): lane i takes words
+// w0 + i, w0 + i + 32, ... of the linear span, or x groups k0 + i, ... of the Morton span.
+__device__ __forceinline__ void write_row_warp(uint32_t* table, bool morton, const uint32_t* grid, int y, int z,
+                                               int xl, int xh, uint32_t lane) {
+	if (morton) {
+		const uint64_t yz = (spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2);
+		for (int k = (xl >> 2) + (int)lane; k <= (xh >> 2); k += 32) {
+			const uint64_t code = spread3((uint32_t)(k << 2)) | yz;
+			const int j0 = max(xl - (k << 2), 0), j1 = min(xh - (k << 2), 3);
+			const uint32_t n = (0xFu << j0) & (0xFu >> (3 - j1));
+			const uint32_t m = ((n & 1u) << 31) | ((n & 2u) << 29) | ((n & 4u) << 21) | ((n & 8u) << 19);
+			atomicOr(table + (code >> 5), m >> (uint32_t)(code & 31u));
+		}
+	} else {
+		const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
+		const uint64_t lo = base + (uint64_t)xl, hi = base + (uint64_t)xh;
+		const uint64_t w0 = lo >> 5, w1 = hi >> 5;
+		for (uint64_t w = w0 + lane; w <= w1; w += 32) {
+			const uint32_t a = (w == w0) ? (uint32_t)(lo & 31u) : 0u;
+			const uint32_t b = (w == w1) ? (uint32_t)(hi & 31u) : 31u;
+			atomicOr(table + w, span_mask(a, b));
+		}
+	}
+}
+
 }  // namespace cvx
