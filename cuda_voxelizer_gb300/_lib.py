@@ -82,6 +82,12 @@ SIGNATURES = {
     "cvx_server_replay": (c_status, [vp, ctypes.POINTER(CvxServerRequest), u32, ctypes.POINTER(ctypes.c_double),
                                      ctypes.POINTER(ctypes.c_double)]),
     "cvx_server_destroy": (c_status, [vp]),
+    "cvx_mesh_bbox_device": (c_status, [vp, u64, vp, vp, vp]),
+    "cvx_voxinfo_from_device": (c_status, [vp, u64, vp, ctypes.POINTER(CvxVoxinfo), vp]),
+    "cvx_gather_soup": (c_status, [vp, u64, vp, u64, vp, vp, vp]),
+    "cvx_transcode": (c_status, [vp, vp, u32, ctypes.c_int, vp]),
+    "cvx_encode_binvox": (c_status, [ctypes.POINTER(CvxVoxinfo), vp, vp, u64, ctypes.POINTER(u64), vp]),
+    "cvx_encode_voxel_list": (c_status, [ctypes.POINTER(CvxVoxinfo), vp, vp, u64, ctypes.POINTER(u64), vp]),
     "cvx_get_tuning": (c_status, [ctypes.c_int, ctypes.POINTER(CvxTuning)]),
     "cvx_set_tuning": (c_status, [ctypes.c_int, ctypes.POINTER(CvxTuning)]),
     "cvx_profile_enable": (c_status, [ctypes.c_int]),

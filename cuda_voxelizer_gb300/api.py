@@ -20,7 +20,9 @@ from ._lib import (CvxError, CvxJob, CvxServerConfig, CvxServerRequest, CvxServe
 
 __all__ = ["VoxInfo", "voxelize", "voxelize_solid", "voxelize_ws", "workspace_size", "create_mesh_bbox_cube",
            "mesh_bbox", "make_voxinfo", "table_words", "Job", "voxelize_batch", "Plan", "device_status",
-           "get_tuning", "set_tuning", "CvxError", "voxelize_host", "profile_enable", "profile_collect", "Server"]
+           "get_tuning", "set_tuning", "CvxError", "voxelize_host", "profile_enable", "profile_collect", "Server",
+           "mesh_bbox_device", "voxinfo_from_device", "gather_soup", "transcode", "encode_binvox", "binvox_header",
+           "encode_voxel_list"]
 
 
 VoxInfo = CvxVoxinfo
@@ -341,3 +343,83 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ---- mesh ingest, layouts and output encoders on the GPU ------------------------------------------
+
+def mesh_bbox_device(triangles, stream=None):
+    """Vertex bounding box of a device triangle soup (CUDA tensor); host float32 arrays."""
+    n = triangles.numel() // 9
+    lo = (ctypes.c_float * 3)()
+    hi = (ctypes.c_float * 3)()
+    check(lib.cvx_mesh_bbox_device(_ptr(triangles), n, lo, hi, _stream(stream)), "cvx_mesh_bbox_device")
+    return np.array(lo[:], dtype=np.float32), np.array(hi[:], dtype=np.float32)
+
+
+def voxinfo_from_device(triangles, gridsize, stream=None) -> VoxInfo:
+    """main()'s setup (bbox, createMeshBBCube, voxinfo) for a device triangle soup."""
+    if np.isscalar(gridsize):
+        gridsize = (gridsize, gridsize, gridsize)
+    g = (ctypes.c_uint32 * 3)(*[int(x) for x in gridsize])
+    info = VoxInfo()
+    check(lib.cvx_voxinfo_from_device(_ptr(triangles), triangles.numel() // 9, g, ctypes.byref(info),
+                                      _stream(stream)), "cvx_voxinfo_from_device")
+    return info
+
+
+def gather_soup(vertices, faces, stream=None):
+    """Indexed mesh (CUDA float32 vertices (V, 3), int32/uint32 faces (F, 3)) -> (soup (F*9,),
+    number of faces with an index out of range).  Synchronizes to read the count."""
+    import torch
+    f = faces.reshape(-1, 3)
+    soup = torch.empty(f.shape[0] * 9, dtype=torch.float32, device=vertices.device)
+    bad = torch.zeros(1, dtype=torch.int64, device=vertices.device)
+    check(lib.cvx_gather_soup(_ptr(vertices), vertices.numel() // 3, _ptr(f), f.shape[0], _ptr(soup), _ptr(bad),
+                              _stream(stream)), "cvx_gather_soup")
+    return soup, int(bad.item())
+
+
+def transcode(table, gridsize: int, to_morton: bool, stream=None):
+    """Morton <-> linear copy of a g^3 table (CUDA tensor); returns a new tensor."""
+    import torch
+    out = torch.empty_like(table)
+    check(lib.cvx_transcode(_ptr(table), _ptr(out), int(gridsize), int(bool(to_morton)), _stream(stream)),
+          "cvx_transcode")
+    return out
+
+
+def encode_binvox(info: VoxInfo, table, stream=None) -> bytes:
+    """binvox run-length payload of a linear-order device table (the bytes after the header)."""
+    import torch
+    n = ctypes.c_uint64()
+    check(lib.cvx_encode_binvox(ctypes.byref(info), _ptr(table), None, 0, ctypes.byref(n), _stream(stream)),
+          "cvx_encode_binvox")
+    out = torch.empty(max(1, n.value), dtype=torch.uint8, device=table.device)
+    check(lib.cvx_encode_binvox(ctypes.byref(info), _ptr(table), _ptr(out), n.value, ctypes.byref(n),
+                                _stream(stream)), "cvx_encode_binvox")
+    return out[:n.value].cpu().numpy().tobytes()
+
+
+def binvox_header(info: VoxInfo) -> bytes:
+    """The ASCII header write_binvox puts before the payload (src/util_io.cpp:209-215), with the
+    stream's default float formatting (6 significant digits)."""
+    lo = [np.float32(v) for v in info.bbox_min]
+    hi = [np.float32(v) for v in info.bbox_max]
+    ext = [np.float32(hi[i] - lo[i]) for i in range(3)]
+    scale = max(max(ext[0], ext[1]), ext[2])
+    g = list(info.gridsize)
+    return (f"#binvox 1\ndim {g[0]} {g[1]} {g[2]}\n"
+            f"translate {'%g' % float(lo[0])} {'%g' % float(lo[1])} {'%g' % float(lo[2])}\n"
+            f"scale {'%g' % float(scale)}\ndata\n").encode()
+
+
+def encode_voxel_list(info: VoxInfo, table, stream=None):
+    """The (x, gz - z, y) int32 triples write_vox hands to its MagicaVoxel writer, in its order."""
+    import torch
+    n = ctypes.c_uint64()
+    check(lib.cvx_encode_voxel_list(ctypes.byref(info), _ptr(table), None, 0, ctypes.byref(n), _stream(stream)),
+          "cvx_encode_voxel_list")
+    out = torch.empty((max(1, n.value), 3), dtype=torch.int32, device=table.device)
+    check(lib.cvx_encode_voxel_list(ctypes.byref(info), _ptr(table), _ptr(out), n.value, ctypes.byref(n),
+                                    _stream(stream)), "cvx_encode_voxel_list")
+    return out[:n.value]

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libcvx.so")
-SOURCES = ["surface.cu", "solid.cu", "api.cu", "dropin.cpp", "microbench.cu", "noalloc.cu", "server.cu", "clear.cu"]
+SOURCES = ["surface.cu", "solid.cu", "api.cu", "dropin.cpp", "microbench.cu", "noalloc.cu", "server.cu", "clear.cu", "mesh.cu", "transcode.cu", "encode.cu"]
 HEADERS = ["cvx_device.cuh", "surface.cuh", "engine.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

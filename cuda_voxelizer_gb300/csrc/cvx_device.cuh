@@ -188,6 +188,30 @@ __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) 
 
 __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
 
+// Inverse of spread3: the bits at positions 0, 3, 6, ... of v, packed.
+__device__ __forceinline__ uint32_t compact3(uint64_t v) {
+	v &= 0x249249249249ull;
+	v = (v ^ (v >> 2)) & 0x0C30C30C30C3ull;
+	v = (v ^ (v >> 4)) & 0x00F00F00F00Full;
+	v = (v ^ (v >> 8)) & 0x0000FF0000FFull;
+	v = (v ^ (v >> 16)) & 0xFFFFull;
+	return (uint32_t)v;
+}
+
+// Morton bit mask of a 4-bit row nibble (x = 4X'..4X'+3 in MSB-first order: nibble bit 3 is dx = 0)
+// for dy = dz = 0.  In a Morton word the code offset of (dx, dy, dz) is
+// (dx&1) | (dy&1)<<1 | dz<<2 | (dx>>1)<<3 | (dy>>1)<<4, and bits are MSB first, so other (dy, dz)
+// shift the mask right by 2*(dy&1) + 4*dz + 16*(dy>>1).
+__device__ __forceinline__ uint32_t nibble_mask(uint32_t nib) {
+	uint32_t m = 0;
+	if (nib & 8u) m |= 0x80000000u;         // dx = 0: offset 0
+	if (nib & 4u) m |= 0x80000000u >> 1;    // dx = 1: offset 1
+	if (nib & 2u) m |= 0x80000000u >> 8;    // dx = 2: offset 8
+	if (nib & 1u) m |= 0x80000000u >> 9;    // dx = 3: offset 9
+	return m;
+}
+
+
 // (int)__fdiv_rn(a, u) (truncation of the correctly rounded quotient, as float3_to_int3 of
 // `a / unit` in the reference, src/util.h:20-22), computed with the per-axis reciprocal inv ~ 1/u.
 // fl(a * inv) is within 2 ulp of fl(a / u); truncation can only differ when the quotient is within

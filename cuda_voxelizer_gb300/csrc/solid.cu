@@ -540,27 +540,7 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 	}
 }
 
-__device__ __forceinline__ uint32_t compact3(uint64_t v) {
-	v &= 0x249249249249ull;
-	v = (v ^ (v >> 2)) & 0x0C30C30C30C3ull;
-	v = (v ^ (v >> 4)) & 0x00F00F00F00Full;
-	v = (v ^ (v >> 8)) & 0x0000FF0000FFull;
-	v = (v ^ (v >> 16)) & 0xFFFFull;
-	return (uint32_t)v;
-}
 
-// Morton bit mask of a 4-bit row nibble (x = 4X'..4X'+3 in MSB-first order: nibble bit 3 is dx = 0)
-// for dy = dz = 0.  In a Morton word the code offset of (dx, dy, dz) is
-// (dx&1) | (dy&1)<<1 | dz<<2 | (dx>>1)<<3 | (dy>>1)<<4, and bits are MSB first, so other (dy, dz)
-// shift the mask right by 2*(dy&1) + 4*dz + 16*(dy>>1).
-__device__ __forceinline__ uint32_t nibble_mask(uint32_t nib) {
-	uint32_t m = 0;
-	if (nib & 8u) m |= 0x80000000u;         // dx = 0: offset 0
-	if (nib & 4u) m |= 0x80000000u >> 1;    // dx = 1: offset 1
-	if (nib & 2u) m |= 0x80000000u >> 8;    // dx = 2: offset 8
-	if (nib & 1u) m |= 0x80000000u >> 9;    // dx = 3: offset 9
-	return m;
-}
 
 // Morton jobs with g >= 32: one CTA per group of W = min(4, g/32) x-adjacent Morton-aligned 32^3
 // bricks.  Each brick is 1,024 consecutive Morton words; the group's 32 x 32 rows of W*32 x-bits are

@@ -189,6 +189,42 @@ cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint
 /* Finishes the queued requests, then frees everything. */
 cvx_status cvx_server_destroy(cvx_server* s);
 
+/* ---- mesh ingest on the GPU (replaces src/main.cpp:61-80 and :179-186) ------------------------ */
+
+/* Vertex bounding box of a device triangle soup (min/max over the 3n vertices, as Trimesh's
+ * need_bbox); synchronizes `stream` and writes the host arrays.  Equal to cvx_mesh_bbox for finite
+ * coordinates. */
+cvx_status cvx_mesh_bbox_device(const float* d_triangles, uint64_t n_triangles, float out_min[3], float out_max[3],
+                                cvx_stream_t stream);
+/* main()'s setup from a device soup: bounding box, createMeshBBCube, voxinfo (synchronizes). */
+cvx_status cvx_voxinfo_from_device(const float* d_triangles, uint64_t n_triangles, const uint32_t gridsize[3],
+                                   cvx_voxinfo* out, cvx_stream_t stream);
+/* Indexed mesh -> soup: face f's vertices d_vertices[3*d_faces[3f+k] ..] become floats 9f..9f+8
+ * of d_soup (the loop of meshToGPU_managed, src/main.cpp:68-77).  A face with an index >=
+ * n_vertices is written as NaNs and counted into *d_bad_faces (device counter, may be NULL);
+ * such a soup must not be voxelized.  Asynchronous. */
+cvx_status cvx_gather_soup(const float* d_vertices, uint64_t n_vertices, const uint32_t* d_faces, uint64_t n_faces,
+                           float* d_soup, unsigned long long* d_bad_faces, cvx_stream_t stream);
+
+/* ---- table layouts and output encoders ------------------------------------------------------ */
+
+/* Morton <-> linear conversion of a g^3 table (g a power of two, 4 <= g <= 65536); source and
+ * destination must not overlap.  to_morton != 0: linear -> Morton.  Asynchronous. */
+cvx_status cvx_transcode(const uint32_t* d_src, uint32_t* d_dst, uint32_t gridsize, int to_morton,
+                         cvx_stream_t stream);
+/* binvox payload of a linear-order table: the (value, count) byte pairs write_binvox emits after
+ * its ASCII header (src/util_io.cpp:219-245: x outermost, then z, then y; runs end on a change or
+ * after 255 voxels).  *out_bytes receives the payload size; with d_out == NULL only the size is
+ * computed, and a capacity below it returns CVX_ERR_INVALID_VALUE.  Synchronizes `stream`; uses
+ * temporary device memory. */
+cvx_status cvx_encode_binvox(const cvx_voxinfo* info, const uint32_t* d_table, uint8_t* d_out, uint64_t out_capacity,
+                             uint64_t* out_bytes, cvx_stream_t stream);
+/* The voxels write_vox hands to VoxWriter::AddVoxel (src/util_io.cpp:264-280), in its order, as
+ * int32 triples (x, gz - z, y) into d_xyz (3 * capacity int32).  Needs gridsize y == z.
+ * *out_count receives the number of set voxels; d_xyz == NULL computes only that.  Synchronizes. */
+cvx_status cvx_encode_voxel_list(const cvx_voxinfo* info, const uint32_t* d_table, int32_t* d_xyz, uint64_t capacity,
+                                 uint64_t* out_count, cvx_stream_t stream);
+
 /* ---- tuning ---------------------------------------------------------------------------------- */
 
 typedef struct cvx_tuning {

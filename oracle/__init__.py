@@ -55,6 +55,10 @@ def lib():
         L.ovx_max_threads.restype = ctypes.c_int
         L.ovx_count_atomics.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.ovx_count_atomics.restype = ctypes.c_uint64
+        L.ovx_binvox_payload.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
+        L.ovx_binvox_payload.restype = ctypes.c_uint64
+        L.ovx_vox_list.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
+        L.ovx_vox_list.restype = ctypes.c_uint64
         _lib = L
     return _lib
 
@@ -112,6 +116,26 @@ def count_atomics(info: bytes, tris, morton: bool = False, solid: bool = False) 
     t = _soup(tris, info)
     ib = ctypes.create_string_buffer(bytes(info), 64)
     return int(lib().ovx_count_atomics(ctypes.addressof(ib), _ptr(t), int(morton), int(solid)))
+
+
+def binvox_payload(info: bytes, table: np.ndarray) -> bytes:
+    """write_binvox's RLE data section for a linear-order table (restatement)."""
+    ib = ctypes.create_string_buffer(bytes(info), 64)
+    t = np.ascontiguousarray(table, dtype=np.uint32)
+    n = int(lib().ovx_binvox_payload(ctypes.addressof(ib), _ptr(t), None, 0))
+    out = np.zeros(max(n, 1), dtype=np.uint8)
+    lib().ovx_binvox_payload(ctypes.addressof(ib), _ptr(t), _ptr(out), n)
+    return out[:n].tobytes()
+
+
+def vox_list(info: bytes, table: np.ndarray) -> np.ndarray:
+    """The (x, gz - z, y) triples write_vox passes to AddVoxel, in order (restatement)."""
+    ib = ctypes.create_string_buffer(bytes(info), 64)
+    t = np.ascontiguousarray(table, dtype=np.uint32)
+    n = int(lib().ovx_vox_list(ctypes.addressof(ib), _ptr(t), None, 0))
+    out = np.zeros((max(n, 1), 3), dtype=np.int32)
+    lib().ovx_vox_list(ctypes.addressof(ib), _ptr(t), _ptr(out), n)
+    return out[:n]
 
 
 def max_threads() -> int:

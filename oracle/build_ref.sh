@@ -6,6 +6,8 @@
 #
 #   libref_cpu.so             src/cpu_voxelizer.cpp (OpenMP CPU voxelizer) + oracle/ref_cpu_shim.cpp,
 #                             host-architecture code, so it is only usable where it was built.
+#   libref_io.so              src/util_io.cpp (output writers) + VoxWriter + oracle/ref_io_shim.cpp,
+#                             host-architecture code (golden-file generation)
 #   ref_voxelize.cubin        src/voxelize.cu        (kernel voxelize_triangle) for sm_103a
 #   ref_voxelize_solid.cubin  src/voxelize_solid.cu  (kernel voxelize_triangle_solid) for sm_103a
 #
@@ -35,6 +37,13 @@ g++ -O2 -fopenmp -std=c++17 -fPIC -shared -w \
     -o "$OUT/libref_cpu.so" &
 pid_cpu=$!
 
+# Reference output writers (src/util_io.cpp with its vendored MagicaVoxel writer), host code.
+g++ -O2 -std=c++17 -fPIC -shared -w -DSILENT \
+    -I"$HERE/trimesh_shim" -I"$REF/src" -I"$CUDA_HOME/include" \
+    "$HERE/ref_io_shim.cpp" "$REF/src/util_io.cpp" "$REF/src/libs/magicavoxel_file_writer/VoxWriter.cpp" \
+    -o "$OUT/libref_io.so" &
+pid_io=$!
+
 # Reference GPU kernels for sm_103a, device code only.
 "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -w \
     -I"$HERE/trimesh_shim" -I"$REF/src" \
@@ -46,6 +55,7 @@ pid_s=$!
 pid_d=$!
 
 wait $pid_cpu
+wait $pid_io
 wait $pid_s
 wait $pid_d
 echo "build_ref: wrote $(ls "$OUT" | tr '\n' ' ')"

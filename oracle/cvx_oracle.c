@@ -465,6 +465,68 @@ int ovx_max_threads(void) {
 #endif
 }
 
+/* ---- output writers (src/util_io.cpp) ------------------------------------------------------ */
+
+/* checkVoxel (src/util.h:25-38): linear index x + y*gx + z*gx*gy, bit 31 - index%32. */
+static int check_voxel(const uint32_t* t, const ovx_info* info, uint64_t x, uint64_t y, uint64_t z) {
+    uint64_t loc = x + y * info->grid[0] + z * (uint64_t)info->grid[0] * info->grid[1];
+    return (t[loc / 32u] >> (31u - (uint32_t)(loc % 32u))) & 1u;
+}
+
+/* write_binvox's data section (src/util_io.cpp:219-245): x, then z, then y; the first voxel's
+ * value, then a count each time the value changes or the count reaches 255, then the value, and
+ * the last count.  Writes at most `cap` bytes to out; returns the number of bytes produced. */
+uint64_t ovx_binvox_payload(const ovx_info* info, const uint32_t* table, uint8_t* out, uint64_t cap) {
+    uint64_t n = 0;
+#define OVX_PUT(b) do { if (n < cap) out[n] = (uint8_t)(b); n++; } while (0)
+    uint8_t current = 0, seen = 0;
+    for (uint64_t x = 0; x < info->grid[0]; x++) {
+        for (uint64_t z = 0; z < info->grid[2]; z++) {
+            for (uint64_t y = 0; y < info->grid[1]; y++) {
+                if (x == 0 && y == 0 && z == 0) {
+                    current = (uint8_t)check_voxel(table, info, 0, 0, 0);
+                    OVX_PUT(current);
+                    seen = 1;
+                    continue;
+                }
+                uint8_t next = (uint8_t)check_voxel(table, info, x, y, z);
+                if (next != current || seen == 255) {
+                    OVX_PUT(seen);
+                    seen = 1;
+                    current = next;
+                    OVX_PUT(current);
+                } else {
+                    seen++;
+                }
+            }
+        }
+    }
+    OVX_PUT(seen);
+#undef OVX_PUT
+    return n;
+}
+
+/* write_vox's voxel loop (src/util_io.cpp:264-280): x, then y over [0, gz), then z over [0, gy);
+ * every set voxel becomes AddVoxel(x, -z + gz, y).  Writes at most cap triples; returns the count. */
+uint64_t ovx_vox_list(const ovx_info* info, const uint32_t* table, int32_t* out, uint64_t cap) {
+    uint64_t n = 0;
+    for (uint64_t x = 0; x < info->grid[0]; x++) {
+        for (uint64_t y = 0; y < info->grid[2]; y++) {
+            for (uint64_t z = 0; z < info->grid[1]; z++) {
+                if (check_voxel(table, info, x, y, z)) {
+                    if (n < cap) {
+                        out[3 * n] = (int32_t)x;
+                        out[3 * n + 1] = (int32_t)(-(int64_t)z + (int64_t)info->grid[2]);
+                        out[3 * n + 2] = (int32_t)y;
+                    }
+                    n++;
+                }
+            }
+        }
+    }
+    return n;
+}
+
 /* createMeshBBCube (src/util.h:80-110) on float3 bounds. */
 void ovx_mesh_bbcube(const float in_min[3], const float in_max[3], float out_min[3], float out_max[3]) {
     float len[3] = {in_max[0] - in_min[0], in_max[1] - in_min[1], in_max[2] - in_min[2]};

@@ -27,6 +27,10 @@ struct TriMesh {
 	};
 	std::vector<point> vertices;
 	std::vector<Face> faces;
+	// File I/O is not provided (only src/util_io.cpp:140,149 names it, in write_obj_cubes, which
+	// the shims never run).
+	static TriMesh* read(const char*) { return nullptr; }
+	bool write(const char*) { return false; }
 };
 
 }  // namespace trimesh
