@@ -383,6 +383,7 @@ def main():
             extras.update(bench_soup(cv, meshgen, torch, stream, flush))
             specs = meshgen.batch_mix(0, 256)
             mix = [(s, s.build()) for s in specs]
+            extras.update(bench_io(cv, meshgen, torch, flush))
             extras.update(bench_batch(cv, torch, mix))
             extras.update(bench_serve(cv, meshgen, torch, mix, args.serve_seconds,
                                       extras["batch_256"]["plan_meshes_s"]))
@@ -465,6 +466,64 @@ def ref_cuda_soup():
     torch.cuda.synchronize()
     ms = a.elapsed_time(b)
     return {"triangles": 2_000_000, "ref_cuda_ms": ms, "ref_cuda_mtris_s": 2.0 / (ms / 1e3)}
+
+
+def bench_io(cv, meshgen, torch, flush):
+    """Ingest, layout and encoder kernels on large inputs, each against the HBM copy rate where it
+    is a streaming kernel: device bbox of the 2M soup (72 MB read), indexed-mesh gather (2M faces
+    of 1M vertices), Morton <-> linear transcode of a 1024^3 table (128 MiB read + 128 MiB
+    written), binvox payload and voxel list of the 512^3 solid icosphere."""
+    hbm, _ = peaks()
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    out = {}
+    soup = torch.from_numpy(meshgen.soup(0, n=2_000_000).reshape(-1)).cuda()
+    ms = timed(lambda: cv.mesh_bbox_device(soup))
+    out["bbox_2m"] = {"ms": ms, "gbs": soup.numel() * 4 / (ms / 1e3) / 1e9, "note": "includes the 24-byte read-back"}
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    verts = torch.rand(1_000_000 * 3, device="cuda", generator=gen)
+    faces = torch.randint(0, 1_000_000, (2_000_000 * 3,), dtype=torch.int32, device="cuda", generator=gen)
+    soup_out = torch.empty(2_000_000 * 9, dtype=torch.float32, device="cuda")
+    from cuda_voxelizer_gb300 import _lib
+    ms = timed(lambda: _lib.lib.cvx_gather_soup(verts.data_ptr(), 1_000_000, faces.data_ptr(), 2_000_000,
+                                                   soup_out.data_ptr(), None, stream.cuda_stream))
+    b = faces.numel() * 4 + soup_out.numel() * 4 + soup_out.numel() * 4
+    out["gather_2m"] = {"ms": ms, "gbs": b / (ms / 1e3) / 1e9, "frac_of_hbm": b / (ms / 1e3) / 1e9 / hbm,
+                        "bytes": b, "note": "faces + soup written + vertices read once per face corner"}
+    g = 1024
+    tab = torch.randint(-2 ** 31, 2 ** 31 - 1, (g ** 3 // 32,), dtype=torch.int32, device="cuda", generator=gen)
+    dst = torch.empty_like(tab)
+    for name, tm in (("linear_to_morton_1024", 1), ("morton_to_linear_1024", 0)):
+        ms = timed(lambda: _lib.lib.cvx_transcode(tab.data_ptr(), dst.data_ptr(), g, tm, stream.cuda_stream))
+        b = 2 * tab.numel() * 4
+        out[name] = {"ms": ms, "gbs": b / (ms / 1e3) / 1e9, "frac_of_hbm": b / (ms / 1e3) / 1e9 / hbm}
+    del tab, dst
+    tris = meshgen.icosphere(0, level=8)
+    info = cv.make_voxinfo(tris, 512)
+    t512 = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+    cv.voxelize_solid(info, torch.from_numpy(tris.reshape(-1)).cuda(), t512)
+    ms = timed(lambda: cv.encode_binvox(info, t512), reps=3)
+    out["binvox_512_solid"] = {"ms": ms, "payload_bytes": len(cv.encode_binvox(info, t512)),
+                               "note": "size pass + emit pass, synchronous, payload copied to the host"}
+    ms = timed(lambda: cv.encode_voxel_list(info, t512), reps=3)
+    out["voxel_list_512_solid"] = {"ms": ms, "voxels": int(cv.encode_voxel_list(info, t512).shape[0])}
+    return {"io": out}
 
 
 def bench_batch(cv, torch, mix):
