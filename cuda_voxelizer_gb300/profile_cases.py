@@ -10,6 +10,8 @@ the ones after.  Cases:
   batch       the 256-mesh uneven mix (triangle counts 1k-500k, grids 64-512, 3:1 surface:solid,
               1:1 linear:Morton) as one cvx_voxelize_batch
   batch_g512  the surface meshes of that mix gridded at 512^3, as one batch
+  io          a random 1024^3 table transcoded linear -> Morton -> linear, then the 512^3 solid
+              icosphere's binvox payload and voxel list
 """
 from __future__ import annotations
 
@@ -83,7 +85,23 @@ def case_batch_g512():
     return run
 
 
-CASES = {"ico8": case_ico8, "soup": case_soup, "batch": case_batch, "batch_g512": case_batch_g512}
+def case_io():
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    tab = torch.randint(-2 ** 31, 2 ** 31 - 1, (1024 ** 3 // 32,), dtype=torch.int32, device="cuda", generator=gen)
+    tris = meshgen.icosphere(0, level=8)
+    info = cv.make_voxinfo(tris, 512)
+    t512 = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+    cv.voxelize_solid(info, torch.from_numpy(tris.reshape(-1)).cuda(), t512)
+
+    def run():
+        m = cv.transcode(tab, 1024, True)
+        cv.transcode(m, 1024, False)
+        cv.encode_binvox(info, t512)
+        cv.encode_voxel_list(info, t512)
+    return run
+
+
+CASES = {"ico8": case_ico8, "soup": case_soup, "batch": case_batch, "batch_g512": case_batch_g512, "io": case_io}
 
 
 def main(argv=None):
