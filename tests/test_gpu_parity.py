@@ -307,3 +307,31 @@ def test_repeated_calls_are_identical():
             outs = [run_engine(info, td, morton, solid) for _ in range(3)]
             torch.cuda.synchronize()
             assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("solid", [False, True])
+def test_mesh_above_one_launch_is_split_exactly(solid):
+    """A mesh of more than 2^24 - 1 triangles runs as several launch groups on one table; by
+    linearity (surface ORs, solid XORs per triangle) it must equal the OR / XOR of its halves."""
+    rng = np.random.default_rng(21)
+    n = (1 << 24) + 12_345
+    base = meshgen.icosphere(8, level=7)  # 327,680 triangles
+    reps = n // base.shape[0] + 1
+    tris = np.concatenate([base + np.tile(rng.normal(0, 0.02, 3), 3).astype(np.float32) for _ in range(reps)])[:n]
+    info = cv.make_voxinfo(tris, 256)
+    d = torch.from_numpy(tris.reshape(-1)).cuda()
+    f = cv.voxelize_solid if solid else cv.voxelize
+    whole = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+    f(info, d, whole)
+    halves = []
+    h = n // 2
+    for a, b in ((0, h), (h, n)):
+        ic = cv.VoxInfo.from_buffer_copy(bytes(info))
+        ic.n_triangles = b - a
+        t = torch.zeros_like(whole)
+        f(ic, d[9 * a:9 * b], t)
+        halves.append(t)
+    want = (halves[0] ^ halves[1]) if solid else (halves[0] | halves[1])
+    torch.cuda.synchronize()
+    assert torch.equal(whole, want)
+    assert int(whole.count_nonzero()) > 0
