@@ -68,26 +68,6 @@ __device__ __forceinline__ void stage_tile(const LaunchDesc& L, const float* src
 	__syncthreads();
 }
 
-// Accumulates bits of consecutive voxels that share a table word, one atomicOr per word.
-struct WordSink {
-	uint32_t* table;
-	uint64_t word = ~0ull;
-	uint32_t mask = 0;
-	__device__ __forceinline__ void add(uint64_t idx) {
-		const uint64_t w = idx >> 5;
-		if (w != word) {
-			if (mask) atomicOr(table + word, mask);
-			word = w;
-			mask = 0;
-		}
-		mask |= bit_of(idx);
-	}
-	__device__ __forceinline__ void flush() {
-		if (mask) atomicOr(table + word, mask);
-		mask = 0;
-	}
-};
-
 // Exclusive prefix sum over the CTA (kTile threads); returns this thread's offset, total in *total.
 __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
 	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -257,16 +237,10 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 		RowK K;
 		row_consts<P>(S, py, pz, K);
 		if (small) {
-			// src/voxelize.cu:136-183: every voxel of the row
-			WordSink sink{table};
-			const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
-			const uint64_t yzm = morton ? ((spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2)) : 0;
-			uint64_t xd = morton ? spread3((uint32_t)S.bx0) : 0;
-			for (int x = S.bx0; x <= S.bx1; x++) {
-				if (voxel_pass<P>(S, K, unit[0], x)) sink.add(morton ? (xd | yzm) : base + (uint64_t)x);
-				if (morton) xd = morton_x_add(xd, kMortonX1);
-			}
-			sink.flush();
+			// src/voxelize.cu:136-183: every voxel of the row (at most 16), as a pass mask
+			uint32_t pm = 0;
+			for (int i = 0; i <= S.bx1 - S.bx0; i++) pm |= (uint32_t)voxel_pass<P>(S, K, unit[0], S.bx0 + i) << i;
+			if (pm) write_row_mask(table, morton, grid, y, z, S.bx0, pm);
 		} else {
 			RowDirs D;
 			row_dirs(S, unit[0], D);

@@ -351,6 +351,39 @@ __device__ __forceinline__ void write_row(uint32_t* table, bool morton, const ui
 	}
 }
 
+// OR the voxels x0 + i of row (y, z) for the set bits i of `pm` (i < 16).  Linear: the run spans at
+// most two words; the bit of voxel idx is 31 - idx % 32, so a word's bits are the bit-reversed mask
+// shifted by the first voxel's offset.  Morton: one word per 4-voxel x-group (offsets {0, 1, 8, 9}
+// from the group's code, as in or_span_morton).
+__device__ __forceinline__ void write_row_mask(uint32_t* table, bool morton, const uint32_t* grid, int y, int z,
+                                               int x0, uint32_t pm) {
+	if (morton) {
+		const uint64_t yz = (spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2);
+		const int x1 = x0 + 31 - __clz(pm);
+		uint64_t xd = spread3((uint32_t)(x0 & ~3));
+		for (int k = x0 >> 2; k <= (x1 >> 2); k++) {
+			const int sh = (k << 2) - x0;  // mask bit of x = 4k
+			const uint32_t n = (sh >= 0 ? pm >> sh : pm << -sh) & 0xFu;
+			if (n) {
+				const uint64_t code = xd | yz;
+				const uint32_t m = ((n & 1u) << 31) | ((n & 2u) << 29) | ((n & 4u) << 21) | ((n & 8u) << 19);
+				atomicOr(table + (code >> 5), m >> (uint32_t)(code & 31u));
+			}
+			xd = morton_x_add(xd, kMortonX4);
+		}
+	} else {
+		const uint64_t idx = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]) + (uint64_t)x0;
+		const uint64_t w = idx >> 5;
+		const uint32_t off = (uint32_t)(idx & 31u);
+		const uint32_t m0 = __brev(pm) >> off;
+		if (m0) atomicOr(table + w, m0);
+		if (off) {
+			const uint32_t m1 = __brev(pm >> (32u - off));
+			if (m1) atomicOr(table + w + 1, m1);
+		}
+	}
+}
+
 // write_row by a whole warp (every lane calls it with the same row): lane i takes words
 // w0 + i, w0 + i + 32, ... of the linear span, or x groups k0 + i, ... of the Morton span.
 __device__ __forceinline__ void write_row_warp(uint32_t* table, bool morton, const uint32_t* grid, int y, int z,
