@@ -684,7 +684,7 @@ def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
     out = {"budget_gib": 40, "seconds_per_rate": seconds, "pool": "256-mesh mix (same as batch_256)",
            "copy_rates": rates, "bytes_per_request": {"in": per_req_in, "out": per_req_out}}
     fr = (0.25, 0.5, 0.75, 0.9)
-    host = {"served": arm(host_pool, 16, 16, fr, 0, 4096), "plain": arm(host_pool, 1, 1, (0.5, 0.9), 10, 512)}
+    host = {"served": arm(host_pool, 4, 32, fr, 0, 4096), "plain": arm(host_pool, 1, 1, (0.5, 0.9), 10, 512)}
     host["roofline_meshes_s"] = min(copy_cap, plan_meshes_s)
     host["served_frac_of_roofline"] = host["served"]["capacity_meshes_s"] / host["roofline_meshes_s"]
     host["served_vs_plain_capacity"] = host["served"]["capacity_meshes_s"] / host["plain"]["capacity_meshes_s"]
