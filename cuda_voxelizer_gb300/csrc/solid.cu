@@ -345,9 +345,11 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 	uint32_t total_cols = 0;
 	const uint32_t off = block_scan(n_cols, s_warp, &total_cols);
 	if (n_cols) {
-		const uint32_t nzc = (sm.small[threadIdx.x].ext >> 16) + 1u;
-		for (uint32_t c = 0; c < n_cols; c++)
-			s_items[off + c] = threadIdx.x | ((c / nzc) << 8) | ((c % nzc) << 16);
+		const uint32_t ext = sm.small[threadIdx.x].ext;
+		const uint32_t nyc = (ext & 0xFFFFu) + 1u, nzc = (ext >> 16) + 1u;
+		uint32_t c = off;
+		for (uint32_t dy = 0; dy < nyc; dy++)
+			for (uint32_t dz = 0; dz < nzc; dz++) s_items[c++] = threadIdx.x | (dy << 8) | (dz << 16);
 	}
 	__syncthreads();
 	for (uint32_t k = threadIdx.x; k < total_cols; k += kTile) {

@@ -206,10 +206,10 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 	// Phase 2: the rows of the tile's small and local triangles, dealt evenly over the CTA.
 	if (n_small) {
 		const SmallTri& o = sm.small[threadIdx.x];
-		const uint32_t ny = ((o.ext >> 8) & 0xFFu) + 1u;
-		const uint32_t off = offs & 0xFFFFu;
-		for (uint32_t r = 0; r < n_small; r++)
-			s_items[off + r] = (uint16_t)(threadIdx.x | ((r % ny) << 8) | ((r / ny) << 12));
+		const uint32_t ny = ((o.ext >> 8) & 0xFFu) + 1u, nz = ((o.ext >> 16) & 0xFFu) + 1u;
+		uint32_t c = offs & 0xFFFFu;
+		for (uint32_t dz = 0; dz < nz; dz++)
+			for (uint32_t dy = 0; dy < ny; dy++) s_items[c++] = (uint16_t)(threadIdx.x | (dy << 8) | (dz << 12));
 	}
 	for (uint32_t r = 0; r < n_local; r++) s_items[loff + r] = (uint16_t)(threadIdx.x | (r << 8));
 	__syncthreads();
