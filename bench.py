@@ -162,6 +162,22 @@ def traffic_from_profiles(kernel: str):
         return None
 
 
+def issue_roofline(kernel, per_launch_ms, clocks):
+    """The dominant kernel against its instruction-issue bound: its warp instructions per launch
+    (ncu, profiles/traffic.json) at 4 per SM per cycle on every SM at the measured clock."""
+    import torch
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            inst = json.load(f)["warp_instructions"][kernel]
+    except Exception:
+        return None
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    t_issue = inst / (sms * 4 * mhz * 1e6)
+    return {"warp_instructions_per_launch": inst, "sms": sms, "sm_mhz": mhz, "t_issue_us": t_issue * 1e6,
+            "t_measured_us": per_launch_ms * 1e3, "frac": t_issue / (per_launch_ms / 1e3)}
+
+
 def step_roofline(cv, torch, T, table_bytes, hbm_gbs, ms_per_step):
     """Roofline of one step by bytes and atomics: per call t = max(B / BW, A / R_atom) with
     B = 36 T + table (+ table again for the solid flip table) and A the exact atomic count of the
@@ -330,6 +346,7 @@ def main():
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "kernel_ms_per_step": kernel_ms, "alg_bytes_per_launch": alg.get(dom, 0),
+                "issue": issue_roofline(dom, per_launch_ms, clk.summary()),
                 "step": step_roofline(cv, torch, T, table_bytes, peak, ms)}
 
     # ---- end to end through the public API with host buffers -------------------------------------
