@@ -335,3 +335,26 @@ def test_mesh_above_one_launch_is_split_exactly(solid):
     torch.cuda.synchronize()
     assert torch.equal(whole, want)
     assert int(whole.count_nonzero()) > 0
+
+
+@pytest.mark.parametrize("morton", [False, True])
+def test_non_finite_vertices_vs_reference_kernel(ref, morton):
+    """Triangles with NaN or infinite vertices, mixed into a normal mesh: the reference kernel's
+    conversions (NaN -> 0, +-inf saturated, then clamped to the grid) and its predicates on NaN
+    (every comparison false) decide which voxels are set; the engine must set the same ones.
+    Surface only: the reference solid kernel writes outside its table for such input."""
+    t = meshgen.icosphere(7, level=3).copy()
+    info = info_of(t, 64)
+    bad = t[:12].copy().reshape(-1, 3, 3)
+    bad[0, 0, 0] = np.nan
+    bad[1, 1, :] = np.nan
+    bad[2, :, :] = np.nan
+    bad[3, 2, 1] = np.inf
+    bad[4, 0, 2] = -np.inf
+    bad[5, 1, 0] = np.inf
+    bad[5, 2, 0] = -np.inf
+    bad[6, 0, :] = np.inf
+    t2 = np.concatenate([t, bad.reshape(-1, 9)[:7]]).astype(np.float32)
+    info.n_triangles = t2.shape[0]
+    a, b = compare(ref, t2, info, morton, False)
+    assert_same(a, b, "non-finite")
