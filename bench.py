@@ -43,7 +43,7 @@ METRIC = "Mtris/s voxelized (icosphere 1.31M tris, 512^3, surface+solid x linear
 SAMPLE_FRACTION = 32
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=400)
@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--no-extras", action="store_true", help="skip the soup / batch / serve side measurements")
     p.add_argument("--serve-seconds", type=float, default=2.0,
                    help="length of each open-loop serving run (the full served configuration uses 60)")
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 def dist_init(n):
