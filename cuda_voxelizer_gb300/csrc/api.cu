@@ -328,6 +328,8 @@ struct Runner {
 	size_t jobs_used = 0;  // JobDesc slots used in the device job area
 	uint64_t cap;          // queue capacity (triangles)
 	size_t jobs_off;
+	bool timed = true;     // per-kernel events for cvx_profile_collect (callers on this thread only)
+	const Prof* p() const { return timed ? prof() : nullptr; }
 
 	cvx_status prepare(Group& g, LaunchDesc& L) {
 		std::memset(&L, 0, sizeof(L));
@@ -365,7 +367,7 @@ struct Runner {
 			cvx_status st = prepare(g, L);
 			if (st != CVX_OK) return st;
 			CVX_CUDA(cudaMemsetAsync(rec, 0, kCountersResetBytes, s));
-			CVX_CUDA(launch_surface(L, dev.tune, dev.rows_grid, s, prof()));
+			CVX_CUDA(launch_surface(L, dev.tune, dev.rows_grid, s, p()));
 		}
 		if (!solid.empty()) {
 			for (Group& g : make_groups(solid, true)) {
@@ -373,13 +375,13 @@ struct Runner {
 				cvx_status st = prepare(g, L);
 				if (st != CVX_OK) return st;
 				CVX_CUDA(cudaMemsetAsync(rec, 0, kCountersResetBytes, s));
-				CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidToggles, prof()));
+				CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidToggles, p()));
 			}
 			Group r = resolve_group(solid);
 			LaunchDesc L;
 			cvx_status st = prepare(r, L);
 			if (st != CVX_OK) return st;
-			CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidResolve, prof()));
+			CVX_CUDA(launch_solid(L, dev.tune, dev.cols_grid, s, kSolidResolve, p()));
 		}
 		return CVX_OK;
 	}
@@ -491,6 +493,7 @@ cvx_status cvx::run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* con
 	         staging_bytes / sizeof(JobDesc)};
 	r.cap = cap;
 	r.jobs_off = lay.jobs;
+	r.timed = false;  // the server's worker thread: nobody collects events there
 	CVX_CUDA(cudaMemsetAsync(d_rec, 0, sizeof(Counters), s));
 	return r.run(surf, solid);
 }
