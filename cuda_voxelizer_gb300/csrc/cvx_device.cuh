@@ -203,12 +203,8 @@ __device__ __forceinline__ uint32_t compact3(uint64_t v) {
 // (dx&1) | (dy&1)<<1 | dz<<2 | (dx>>1)<<3 | (dy>>1)<<4, and bits are MSB first, so other (dy, dz)
 // shift the mask right by 2*(dy&1) + 4*dz + 16*(dy>>1).
 __device__ __forceinline__ uint32_t nibble_mask(uint32_t nib) {
-	uint32_t m = 0;
-	if (nib & 8u) m |= 0x80000000u;         // dx = 0: offset 0
-	if (nib & 4u) m |= 0x80000000u >> 1;    // dx = 1: offset 1
-	if (nib & 2u) m |= 0x80000000u >> 8;    // dx = 2: offset 8
-	if (nib & 1u) m |= 0x80000000u >> 9;    // dx = 3: offset 9
-	return m;
+	// dx = 0, 1 (nibble bits 3, 2) -> offsets 0, 1 (bits 31, 30); dx = 2, 3 (bits 1, 0) -> offsets 8, 9
+	return ((nib & 0xCu) << 28) | ((nib & 0x3u) << 22);
 }
 
 
