@@ -255,7 +255,7 @@ void finish_group(Group& g, bool solid) {
 				if (morton_slab_grid(gx)) {
 					ms += (gx / 16) * (gx / 16);  // slabs of 16 x 16 rows
 					const uint32_t stride = (uint32_t)(gx / 32) | 1u;
-					g.slab_smem = std::max(g.slab_smem, 256u * stride * 4u);
+					g.slab_smem = std::max(g.slab_smem, (256u * stride + kSlabSkewWords) * 4u);
 				} else if (gx >= 32) {
 					const uint64_t w = gx >= 128 ? 4 : gx / 32;  // x-adjacent 32^3 bricks per CTA
 					mb += (vox >> 15) / w;

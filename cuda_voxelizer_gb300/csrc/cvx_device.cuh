@@ -188,6 +188,13 @@ __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) 
 
 __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
 
+// Shared-memory slab of 256 rows (16 z-slices x 16 rows) of `stride` (odd) words: row r starts at
+// r * stride + r / 32.  The odd stride spreads consecutive rows over the banks; the skew of one word
+// per 32 rows does the same for rows 32 apart, which a Morton gather reads together (a word of a
+// 16^3 block touches rows (2Z + dz) * 16 + 4Y + dy).
+__host__ __device__ __forceinline__ uint32_t slab_row(uint32_t r, uint32_t stride) { return r * stride + (r >> 5); }
+constexpr uint32_t kSlabSkewWords = 256 / 32;  // extra words of a 256-row slab
+
 // Inverse of spread3: the bits at positions 0, 3, 6, ... of v, packed.
 __device__ __forceinline__ uint32_t compact3(uint64_t v) {
 	v &= 0x249249249249ull;

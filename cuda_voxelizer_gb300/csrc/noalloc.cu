@@ -170,7 +170,7 @@ extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const 
 	if (morton) {
 		if (morton_slab_grid(g0)) {
 			L.n_mslabs = (g0 / 16) * (g0 / 16);
-			L.slab_smem = 256u * ((uint32_t)(g0 / 32) | 1u) * 4u;
+			L.slab_smem = (256u * ((uint32_t)(g0 / 32) | 1u) + kSlabSkewWords) * 4u;
 		} else if (g0 >= 32) {
 			L.n_mbricks = ((g0 * g1 * g2) >> 15) / (g0 >= 128 ? 4 : g0 / 32);
 		} else {

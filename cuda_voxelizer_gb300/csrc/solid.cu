@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant_
 // resolves one whole row (prefix XOR along x); then every 16^3 block along x -- 128 consecutive
 // Morton words -- is gathered from 4-bit row nibbles and XORed into the table.
 __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__ LaunchDesc L) {
-	extern __shared__ __align__(16) uint32_t s_slab[];  // [row = zi*16 + yi][stride]
+	extern __shared__ __align__(16) uint32_t s_slab[];  // row zi*16 + yi at slab_row(row, stride)
 	const uint64_t slab = blockIdx.x;
 	const uint32_t j = job_search(L, slab, [](const JobDesc& d) { return d.mslab_begin; });
 	const JobDesc& J = job_at(L, j);
@@ -632,13 +632,13 @@ __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__
 #pragma unroll
 		for (int k = 0; k < 4; k++) {
 			const uint32_t idx = 4 * q + k;
-			s_slab[(zi * 16 + (idx >> lgw)) * stride + (idx & (wpr - 1u))] = vv[k];
+			s_slab[slab_row(zi * 16 + (idx >> lgw), stride) + (idx & (wpr - 1u))] = vv[k];
 		}
 		if (v.x | v.y | v.z | v.w) *src = make_uint4(0u, 0u, 0u, 0u);
 	}
 	__syncthreads();
 	{
-		uint32_t* row = s_slab + threadIdx.x * stride;  // 256 rows, one per thread
+		uint32_t* row = s_slab + slab_row(threadIdx.x, stride);  // 256 rows, one per thread
 		uint32_t carry = 0;
 		for (uint32_t w = 0; w < wpr; w++) {
 			const uint32_t t = row[w];
@@ -658,7 +658,7 @@ __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__
 		for (uint32_t dz = 0; dz < 2; dz++)
 #pragma unroll
 			for (uint32_t dy = 0; dy < 4; dy++) {
-				const uint32_t rw = s_slab[((2 * Z + dz) * 16 + 4 * Y + dy) * stride + wsel];
+				const uint32_t rw = s_slab[slab_row((2 * Z + dz) * 16 + 4 * Y + dy, stride) + wsel];
 				const uint32_t nib = (rw >> (28u - xoff)) & 0xFu;
 				out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 			}
@@ -748,7 +748,7 @@ static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int col
 			cudaGetDevice(&dev);
 			if (dev >= 0 && dev < 64 && !attr_set[dev]) {
 				if ((e = cudaFuncSetAttribute(solid_morton_slab, cudaFuncAttributeMaxDynamicSharedMemorySize,
-				                              256 * (32 + 1) * 4)) != cudaSuccess)
+				                              (256 * (32 + 1) + kSlabSkewWords) * 4)) != cudaSuccess)
 					return e;
 				attr_set[dev] = 1;
 			}

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) linear_to_morton_slab(const uint32_t* __r
 #pragma unroll
 		for (int k = 0; k < 4; k++) {
 			const uint32_t idx = 4 * q + k;
-			s_rows[(zi * 16 + idx / wpr) * stride + idx % wpr] = vv[k];
+			s_rows[slab_row(zi * 16 + idx / wpr, stride) + idx % wpr] = vv[k];
 		}
 	}
 	__syncthreads();
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) linear_to_morton_slab(const uint32_t* __r
 		for (uint32_t dz = 0; dz < 2; dz++)
 #pragma unroll
 			for (uint32_t dy = 0; dy < 4; dy++) {
-				const uint32_t rw = s_rows[((2 * Z + dz) * 16 + 4 * Y + dy) * stride + wsel];
+				const uint32_t rw = s_rows[slab_row((2 * Z + dz) * 16 + 4 * Y + dy, stride) + wsel];
 				out |= nibble_mask((rw >> (28u - xoff)) & 0xFu) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 			}
 		mor[(slab_block(bx, by, bz) << 7) + m] = out;
@@ -174,9 +174,10 @@ extern "C" cvx_status cvx_transcode(const uint32_t* d_src, uint32_t* d_dst, uint
 		int dev = 0;
 		cudaGetDevice(&dev);
 		const uint32_t wpr = gridsize >> 5, nb = gridsize >> 4;
-		const size_t smem_l2m = 256u * (wpr | 1u) * 4u, smem_m2l = nb * 129u * 4u;
+		const size_t smem_l2m = (256u * (wpr | 1u) + kSlabSkewWords) * 4u, smem_m2l = nb * 129u * 4u;
 		if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-			cudaFuncSetAttribute(linear_to_morton_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 33 * 4);
+			cudaFuncSetAttribute(linear_to_morton_slab, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                     (256 * 33 + kSlabSkewWords) * 4);
 			cudaFuncSetAttribute(morton_to_linear_slab, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 129 * 4);
 			attr_set[dev] = true;
 		}
