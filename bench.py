@@ -10,6 +10,7 @@ Keys beyond the base contract:
   e2e          the same metric through the public host-buffer path: pinned host triangles copied in,
                four voxelizations, four tables copied out, all inside the timed region; copies run
                on a second stream, overlapped with the voxelizations that do not need them.
+  step_as_plan the same four calls as one cvx_plan (CUDA graph) launch: the batch form of the step.
   roofline     the step's dominant kernel against the measured HBM copy bandwidth
                (MEASURED_PEAKS.json), with DRAM traffic from the committed ncu summary when present.
   cpu_baseline the reference CPU algorithm (oracle port, OpenMP with a critical section per bit, as
@@ -318,6 +319,28 @@ def main():
     ms = total_ms / args.steps
     value = world * 4 * T * args.steps / (total_ms / 1e3) / 1e6
 
+    # ---- the same step as one CUDA-graph plan (the batch form: 4 jobs, tables cleared in-graph) ---
+    plan = cv.Plan([cv.Job(info, d_tris, tab, morton, solid) for (morton, solid), tab in zip(MODES, tables)],
+                   clear_tables=True)
+    for _ in range(3):
+        plan.launch()
+    torch.cuda.synchronize()
+    plan_times = []
+    for _ in range(min(args.steps, 100)):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        plan.launch()
+        b.record(stream)
+        torch.cuda.synchronize()
+        plan_times.append(a.elapsed_time(b))
+    plan_ms = float(np.mean(plan_times))
+    plan.close()
+    step_plan = {"ms_per_step": plan_ms, "value": 4 * T / (plan_ms / 1e3) / 1e6, "unit": "Mtris/s",
+                 "note": "the 4 calls as one cvx_plan graph launch (surface and solid chains on two captured streams)"}
+
     # ---- per-kernel times for the roofline ------------------------------------------------------
     cv.profile_enable(True)
     prof = {}
@@ -425,7 +448,7 @@ def main():
                                    "per step", "gridsize": 512, "triangles": T, "l2": "flushed between steps "
                                    "(512 MiB write, untimed)", "parallelism": f"replicas x{world}"},
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps, "e2e": e2e,
-            "roofline": roofline}
+            "roofline": roofline, "step_as_plan": step_plan}
 
     if rank == 0:
         import oracle
