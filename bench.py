@@ -339,7 +339,7 @@ def main():
     plan_ms = float(np.mean(plan_times))
     plan.close()
     step_plan = {"ms_per_step": plan_ms, "value": 4 * T / (plan_ms / 1e3) / 1e6, "unit": "Mtris/s",
-                 "note": "the 4 calls as one cvx_plan graph launch (surface and solid chains on two captured streams)"}
+                 "note": "the 4 calls as one cvx_plan graph launch (surface and solid lanes on parallel captured streams)"}
 
     # ---- per-kernel times for the roofline ------------------------------------------------------
     cv.profile_enable(True)

@@ -681,12 +681,17 @@ cvx_status cvx_voxelize_batch(const cvx_job* jobs, uint32_t n_jobs, cvx_stream_t
 struct cvx_plan {
 	cudaGraphExec_t exec = nullptr;
 	cudaGraph_t graph = nullptr;
-	void* rec = nullptr;
-	void* rec_solid = nullptr;     // counters and queues of the solid chain (runs beside the surface chain)
+	std::vector<void*> recs;       // counters and queues of each lane
+	JobDesc* job_area = nullptr;   // the job arrays of every lane's multi-job launches
 	uint32_t* flips = nullptr;
-	JobDesc* staging = nullptr;
 	ClearRange* clears = nullptr;  // the tables the graph zeroes (CVX_PLAN_CLEAR_TABLES)
 };
+
+// A plan runs its jobs in lanes: the surface jobs split into up to kPlanSurfaceLanes groups of
+// about equal triangle count, and the solid jobs in one more.  Each lane has its own counters and
+// queues and its own captured stream, so the graph lets the lanes' kernels overlap (a lane's
+// latency-bound cooperative kernel runs beside another lane's classify kernel).
+constexpr int kPlanSurfaceLanes = 2;
 
 cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out) {
 	if (!out) return fail(CVX_ERR_INVALID_VALUE, "out is null");
@@ -710,21 +715,33 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		cvx_plan_destroy(p);
 		return s2;
 	};
+
+	struct Lane {
+		bool solid = false;
+		std::vector<JobDesc> jobs;
+		std::vector<Group> groups;  // toggles / surface launches; the solid lane's resolve is last
+		uint64_t cap = 1;
+		size_t job_off = 0;          // first JobDesc slot of the lane in the job area
+		cudaStream_t stream = nullptr;
+		cudaEvent_t done = nullptr;
+	};
+	std::vector<Lane> lanes;
+	if (!surf.empty()) {
+		const size_t k = std::min<size_t>(kPlanSurfaceLanes, surf.size());
+		std::vector<Lane> sl(k);
+		std::vector<uint64_t> load(k, 0);
+		std::vector<size_t> order(surf.size());
+		for (size_t i = 0; i < order.size(); i++) order[i] = i;
+		std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return surf[x].n_tri > surf[y].n_tri; });
+		for (size_t i : order) {
+			const size_t b = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+			sl[b].jobs.push_back(surf[i]);
+			load[b] += surf[i].n_tri;
+		}
+		for (Lane& l : sl) lanes.push_back(std::move(l));
+	}
 	uint64_t flip_total = 0;
 	for (const JobDesc& j : solid) flip_total += flip_bytes_of(j);
-	const uint64_t cap = queue_cap(surf, {});
-	const uint64_t cap_solid = queue_cap({}, solid);
-	const size_t slots = job_slots(surf, solid);
-	const RecLayout lay = rec_layout(cap, slots);
-	const RecLayout lay_solid = rec_layout(cap_solid, 0);
-	if (cudaMalloc(&p->rec, lay.end) != cudaSuccess) {
-		cudaGetLastError();
-		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
-	}
-	if (!solid.empty() && cudaMalloc(&p->rec_solid, lay_solid.end) != cudaSuccess) {
-		cudaGetLastError();
-		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
-	}
 	if (flip_total) {
 		if (cudaMalloc((void**)&p->flips, flip_total) != cudaSuccess) {
 			cudaGetLastError();
@@ -733,8 +750,46 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		if (cudaMemset(p->flips, 0, flip_total) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "memset"));
 		assign_flips(solid, p->flips);
 	}
-	if (slots && cudaMallocHost((void**)&p->staging, slots * sizeof(JobDesc)) != cudaSuccess)
-		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan staging"));
+	if (!solid.empty()) {
+		Lane l;
+		l.solid = true;
+		l.jobs = solid;
+		lanes.push_back(std::move(l));
+	}
+	size_t slots = 0;
+	for (Lane& l : lanes) {
+		l.groups = make_groups(l.jobs, l.solid);
+		if (l.solid) l.groups.push_back(resolve_group(l.jobs));
+		l.job_off = slots;
+		for (size_t gi = 0; gi < l.groups.size(); gi++) {
+			const Group& g = l.groups[gi];
+			if (!(l.solid && gi + 1 == l.groups.size())) l.cap = std::max<uint64_t>(l.cap, g.tris);
+			if (g.jobs.size() > 1) slots += g.jobs.size();
+		}
+	}
+	if (slots) {
+		if (cudaMalloc((void**)&p->job_area, slots * sizeof(JobDesc)) != cudaSuccess) {
+			cudaGetLastError();
+			return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan job arrays"));
+		}
+		size_t used = 0;
+		for (const Lane& l : lanes)
+			for (const Group& g : l.groups) {
+				if (g.jobs.size() <= 1) continue;
+				if (cudaMemcpy(p->job_area + used, g.jobs.data(), g.jobs.size() * sizeof(JobDesc), cudaMemcpyHostToDevice) !=
+				    cudaSuccess)
+					return bail(cuda_fail(cudaGetLastError(), "job upload"));
+				used += g.jobs.size();
+			}
+	}
+	for (const Lane& l : lanes) {
+		void* rec = nullptr;
+		if (cudaMalloc(&rec, rec_layout(l.cap, 0).end) != cudaSuccess) {
+			cudaGetLastError();
+			return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
+		}
+		p->recs.push_back(rec);
+	}
 	std::vector<ClearRange> clears;
 	uint32_t clear_total = 0;
 	if (flags & CVX_PLAN_CLEAR_TABLES) {
@@ -752,69 +807,57 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 				return bail(cuda_fail(cudaGetLastError(), "clear list upload"));
 		}
 	}
-	cudaStream_t cs, cs2;
-	cudaEvent_t fork_ev, join_ev;
+
+	cudaStream_t cs;
+	cudaEvent_t fork_ev;
 	if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "stream"));
-	if (cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking) != cudaSuccess) {
-		cudaStreamDestroy(cs);
-		return bail(cuda_fail(cudaGetLastError(), "stream"));
-	}
 	cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming);
-	cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming);
-	auto drop_streams = [&]() {
-		cudaStreamDestroy(cs);
-		cudaStreamDestroy(cs2);
-		cudaEventDestroy(fork_ev);
-		cudaEventDestroy(join_ev);
-	};
-	// Upload the job arrays once, outside the graph (the graph only reads them), in the order the
-	// capture below consumes them.
-	{
-		size_t used = 0;
-		auto upload = [&](const std::vector<Group>& gs) -> cvx_status {
-			for (const Group& g : gs) {
-				if (g.jobs.size() <= 1) continue;
-				JobDesc* devp = reinterpret_cast<JobDesc*>(static_cast<char*>(p->rec) + lay.jobs) + used;
-				if (cudaMemcpy(devp, g.jobs.data(), g.jobs.size() * sizeof(JobDesc), cudaMemcpyHostToDevice) != cudaSuccess)
-					return cuda_fail(cudaGetLastError(), "job upload");
-				used += g.jobs.size();
+	const bool fork = lanes.size() > 1;
+	cvx_status cst = CVX_OK;
+	for (Lane& l : lanes) {
+		l.stream = cs;
+		if (fork && cst == CVX_OK) {
+			if (cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking) != cudaSuccess ||
+			    cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming) != cudaSuccess) {
+				l.stream = cs;
+				cst = cuda_fail(cudaGetLastError(), "stream");
 			}
-			return CVX_OK;
-		};
-		cvx_status s2 = upload(make_groups(surf, false));
-		if (s2 == CVX_OK && !solid.empty()) s2 = upload(make_groups(solid, true));
-		if (s2 == CVX_OK && solid.size() > 1) {
-			std::vector<Group> rg{resolve_group(solid)};
-			s2 = upload(rg);
 		}
-		if (s2 != CVX_OK) {
-			drop_streams();
-			return bail(s2);
+	}
+	auto drop_streams = [&]() {
+		for (Lane& l : lanes) {
+			if (l.stream && l.stream != cs) cudaStreamDestroy(l.stream);
+			if (l.done) cudaEventDestroy(l.done);
 		}
+		cudaStreamDestroy(cs);
+		cudaEventDestroy(fork_ev);
+	};
+	if (cst != CVX_OK) {
+		drop_streams();
+		return bail(cst);
 	}
 	if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
 		drop_streams();
 		return bail(cuda_fail(cudaGetLastError(), "begin capture"));
 	}
-	cvx_status cst = CVX_OK;
 	if (!clears.empty() && launch_clear(p->clears, (uint32_t)clears.size(), clear_total, cs) != cudaSuccess)
 		cst = cuda_fail(cudaGetLastError(), "table clear");
-	if (cst == CVX_OK && cudaMemsetAsync(p->rec, 0, sizeof(Counters), cs) != cudaSuccess)
-		cst = cuda_fail(cudaGetLastError(), "counter clear");
-	// The solid chain runs on a second captured stream with its own counters and queues, so the
-	// graph lets it overlap the surface chain (they touch different tables).
-	const bool fork = cst == CVX_OK && !solid.empty() && !surf.empty();
-	cudaStream_t ss = fork ? cs2 : cs;
-	if (fork && (cudaEventRecord(fork_ev, cs) != cudaSuccess || cudaStreamWaitEvent(cs2, fork_ev, 0) != cudaSuccess))
-		cst = cuda_fail(cudaGetLastError(), "capture fork");
-	if (cst == CVX_OK && p->rec_solid && cudaMemsetAsync(p->rec_solid, 0, sizeof(Counters), ss) != cudaSuccess)
-		cst = cuda_fail(cudaGetLastError(), "counter clear");
-	if (cst == CVX_OK) {
-		// Launch exactly like Runner::run, but with the job arrays already resident.
-		size_t used = 0;
-		void* rec_now = p->rec;
-		uint64_t cap_now = cap;
-		auto prep = [&](Group& g, LaunchDesc& L) {
+	if (cst == CVX_OK && fork && cudaEventRecord(fork_ev, cs) != cudaSuccess) cst = cuda_fail(cudaGetLastError(), "capture fork");
+	// Launch exactly like Runner::run, but with the job arrays already resident.
+	for (size_t li = 0; li < lanes.size() && cst == CVX_OK; li++) {
+		Lane& l = lanes[li];
+		void* rec = p->recs[li];
+		const RecLayout l0 = rec_layout(l.cap, 0);
+		if ((fork && cudaStreamWaitEvent(l.stream, fork_ev, 0) != cudaSuccess) ||
+		    cudaMemsetAsync(rec, 0, sizeof(Counters), l.stream) != cudaSuccess) {
+			cst = cuda_fail(cudaGetLastError(), "capture lane");
+			break;
+		}
+		size_t used = l.job_off;
+		for (size_t gi = 0; gi < l.groups.size() && cst == CVX_OK; gi++) {
+			Group& g = l.groups[gi];
+			const bool resolve = l.solid && gi + 1 == l.groups.size();
+			LaunchDesc L;
 			std::memset(&L, 0, sizeof(L));
 			L.n_jobs = (uint32_t)g.jobs.size();
 			L.n_tiles = g.tiles;
@@ -823,51 +866,31 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 			L.n_mbricks = g.mbricks;
 			L.n_mslabs = g.mslabs;
 			L.slab_smem = g.slab_smem;
-			L.scr.ctr = reinterpret_cast<Counters*>(rec_now);
-			const RecLayout l0 = rec_layout(cap_now, 0);
-			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(rec_now) + l0.big);
-			L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(rec_now) + l0.mid);
-			L.scr.cap = (uint32_t)cap_now;
+			L.scr.ctr = reinterpret_cast<Counters*>(rec);
+			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(rec) + l0.big);
+			L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(rec) + l0.mid);
+			L.scr.cap = (uint32_t)l.cap;
 			if (g.jobs.size() == 1) {
 				L.single = g.jobs[0];
 			} else {
-				L.jobs = reinterpret_cast<JobDesc*>(static_cast<char*>(p->rec) + lay.jobs) + used;
+				L.jobs = p->job_area + used;
 				used += g.jobs.size();
 			}
-		};
-		for (Group& g : make_groups(surf, false)) {
-			LaunchDesc L;
-			prep(g, L);
-			if (cudaMemsetAsync(p->rec, 0, kCountersResetBytes, cs) != cudaSuccess ||
-			    launch_surface(L, dev.tune, dev.rows_grid, cs, nullptr) != cudaSuccess) {
-				cst = cuda_fail(cudaGetLastError(), "capture surface");
-				break;
+			cudaError_t e = cudaSuccess;
+			if (resolve) {
+				e = launch_solid(L, dev.tune, dev.cols_grid, l.stream, kSolidResolve, nullptr);
+			} else {
+				e = cudaMemsetAsync(rec, 0, kCountersResetBytes, l.stream);
+				if (e == cudaSuccess)
+					e = l.solid ? launch_solid(L, dev.tune, dev.cols_grid, l.stream, kSolidToggles, nullptr)
+					            : launch_surface(L, dev.tune, dev.rows_grid, l.stream, nullptr);
 			}
+			if (e != cudaSuccess) cst = cuda_fail(e, "capture launch");
 		}
-		if (cst == CVX_OK && !solid.empty()) {
-			rec_now = p->rec_solid;
-			cap_now = cap_solid;
-			for (Group& g : make_groups(solid, true)) {
-				LaunchDesc L;
-				prep(g, L);
-				if (cudaMemsetAsync(p->rec_solid, 0, kCountersResetBytes, ss) != cudaSuccess ||
-				    launch_solid(L, dev.tune, dev.cols_grid, ss, kSolidToggles, nullptr) != cudaSuccess) {
-					cst = cuda_fail(cudaGetLastError(), "capture solid");
-					break;
-				}
-			}
-			if (cst == CVX_OK) {
-				Group rg = resolve_group(solid);
-				LaunchDesc L;
-				prep(rg, L);
-				if (launch_solid(L, dev.tune, dev.cols_grid, ss, kSolidResolve, nullptr) != cudaSuccess)
-					cst = cuda_fail(cudaGetLastError(), "capture resolve");
-			}
-		}
+		if (cst == CVX_OK && fork &&
+		    (cudaEventRecord(l.done, l.stream) != cudaSuccess || cudaStreamWaitEvent(cs, l.done, 0) != cudaSuccess))
+			cst = cuda_fail(cudaGetLastError(), "capture join");
 	}
-	if (fork && (cudaEventRecord(join_ev, cs2) != cudaSuccess || cudaStreamWaitEvent(cs, join_ev, 0) != cudaSuccess) &&
-	    cst == CVX_OK)
-		cst = cuda_fail(cudaGetLastError(), "capture join");
 	cudaGraph_t graph = nullptr;
 	cudaError_t ee = cudaStreamEndCapture(cs, &graph);
 	drop_streams();
@@ -892,10 +915,9 @@ cvx_status cvx_plan_destroy(cvx_plan* p) {
 	if (!p) return CVX_OK;
 	if (p->exec) cudaGraphExecDestroy(p->exec);
 	if (p->graph) cudaGraphDestroy(p->graph);
-	if (p->rec) cudaFree(p->rec);
-	if (p->rec_solid) cudaFree(p->rec_solid);
+	for (void* r : p->recs) cudaFree(r);
+	if (p->job_area) cudaFree(p->job_area);
 	if (p->flips) cudaFree(p->flips);
-	if (p->staging) cudaFreeHost(p->staging);
 	if (p->clears) cudaFree(p->clears);
 	delete p;
 	return CVX_OK;
