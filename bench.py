@@ -301,7 +301,6 @@ def main():
         step()
     torch.cuda.synchronize()
     barrier(world)
-    launches_per_step = 2 + 2 + 3 + 5  # surface: classify+rows; solid: classify+cols+resolve (+morton+zero)
     times = []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -355,6 +354,7 @@ def main():
     cv.profile_enable(False)
     kernel_ms = {k: float(np.sum(v)) / reps for k, v in prof.items()}
     launches = {k: len(v) // reps for k, v in prof.items()}
+    launches_per_step = sum(launches.values())  # the engine's kernels in one step, counted by its events
     dom = max(kernel_ms, key=kernel_ms.get)
     # algorithmic bytes per launch: triangles read once (36 B each) + the table (g^3/8) for the
     # classify kernels; flip table read + table write (2 g^3/8) for the solid resolve.
