@@ -180,10 +180,11 @@ def issue_roofline(kernel, per_launch_ms, clocks):
 
 
 def step_roofline(cv, torch, T, table_bytes, hbm_gbs, ms_per_step):
-    """Roofline of one step by bytes and atomics: per call t = max(B / BW, A / R_atom) with
-    B = 36 T + table (+ table again for the solid flip table) and A the exact atomic count of the
-    workload (profiles/atomic_terms.json, counted by the oracle); R_atom is the scattered 32-bit
-    atomicOr rate measured here on a 128 MiB table."""
+    """Roofline of one step by bytes and atomics.  The 4 calls run concurrently and share HBM and
+    the L2 atomic units, so t = max(sum B / BW, sum A / R_atom) with per call B = 36 T + table
+    (+ table again for the solid flip table) and A the exact atomic count of the workload
+    (profiles/atomic_terms.json, counted by the oracle); R_atom is the scattered 32-bit atomicOr
+    rate measured here on a 128 MiB table."""
     from cuda_voxelizer_gb300 import _lib
     try:
         with open(os.path.join(ROOT, "profiles", "atomic_terms.json")) as f:
@@ -194,14 +195,16 @@ def step_roofline(cv, torch, T, table_bytes, hbm_gbs, ms_per_step):
     buf = torch.zeros(words, dtype=torch.int32, device="cuda")
     r_atom = max(_lib.lib.cvx_microbench_atomic_or(buf.data_ptr(), words, 0, 152 * 8, 64) for _ in range(3))
     del buf
-    calls, t_roof = {}, 0.0
+    calls, sum_b, sum_a = {}, 0.0, 0.0
     for (morton, solid), name in zip(MODES, ("surface_linear", "surface_morton", "solid_linear", "solid_morton")):
         b = 36 * T + table_bytes * (2 if solid else 1)
         a = int(terms[name])
         tb, ta = b / (hbm_gbs * 1e9), a / r_atom
         calls[name] = {"bytes": b, "atomics": a, "t_bytes_us": tb * 1e6, "t_atomics_us": ta * 1e6}
-        t_roof += max(tb, ta)
-    return {"definition": "sum over the 4 calls of max(B/BW_hbm, A/R_atom)", "r_atom_per_s": r_atom,
+        sum_b += tb
+        sum_a += ta
+    t_roof = max(sum_b, sum_a)
+    return {"definition": "max(sum over the 4 calls of B/BW_hbm, sum of A/R_atom)", "r_atom_per_s": r_atom,
             "hbm_gbs": hbm_gbs, "calls": calls, "t_roof_us": t_roof * 1e6, "t_measured_us": ms_per_step * 1e3,
             "frac": t_roof / (ms_per_step / 1e3)}
 
@@ -291,10 +294,25 @@ def main():
     tables = [torch.empty(W, dtype=torch.int32, device="cuda") for _ in MODES]
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
-    def step():
+    def step_seq():
         for (morton, solid), tab in zip(MODES, tables):
             tab.zero_()
             (cv.voxelize_solid if solid else cv.voxelize)(info, d_tris, tab, morton)
+
+    # The timed step: the 4 calls on 4 streams (each stream has its own queues and counters in the
+    # engine), forked from and joined back into the timing stream.
+    side = [torch.cuda.Stream() for _ in MODES]
+
+    def step():
+        fork = torch.cuda.Event()
+        fork.record(stream)
+        for (morton, solid), tab, s in zip(MODES, tables, side):
+            s.wait_event(fork)
+            with torch.cuda.stream(s):
+                tab.zero_()
+                (cv.voxelize_solid if solid else cv.voxelize)(info, d_tris, tab, morton, stream=s)
+        for s in side:
+            stream.wait_stream(s)
 
     # ---- device-resident throughput -------------------------------------------------------------
     for _ in range(max(3, args.warmup)):
@@ -337,6 +355,20 @@ def main():
         plan_times.append(a.elapsed_time(b))
     plan_ms = float(np.mean(plan_times))
     plan.close()
+    seq_times = []
+    for _ in range(min(args.steps, 100)):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step_seq()
+        b.record(stream)
+        torch.cuda.synchronize()
+        seq_times.append(a.elapsed_time(b))
+    seq_ms = float(np.mean(seq_times))
+    step_seq_line = {"ms_per_step": seq_ms, "value": 4 * T / (seq_ms / 1e3) / 1e6, "unit": "Mtris/s",
+                     "note": "the 4 calls one after another on one stream"}
     step_plan = {"ms_per_step": plan_ms, "value": 4 * T / (plan_ms / 1e3) / 1e6, "unit": "Mtris/s",
                  "note": "the 4 calls as one cvx_plan graph launch (surface and solid lanes on parallel captured streams)"}
 
@@ -347,7 +379,7 @@ def main():
     for _ in range(reps):
         flush.fill_(1)
         torch.cuda.synchronize()
-        step()
+        step_seq()
         torch.cuda.synchronize()
         for name, t in cv.profile_collect():
             prof.setdefault(name, []).append(t)
@@ -376,44 +408,39 @@ def main():
     h_tris = torch.from_numpy(tris.reshape(-1)).pin_memory()
     h_out = [torch.empty(W, dtype=torch.int32).pin_memory() for _ in MODES]
 
-    # Two streams: the triangles go up in 4 chunks on the copy stream and the first call (surface,
-    # linear) voxelizes each chunk as it lands (the table accumulates: same bits as one call); each
-    # table goes down on the copy stream while the next call runs.
-    copy_stream = torch.cuda.Stream()
-    n_chunks = 4
-    bounds = [T * c // n_chunks for c in range(n_chunks + 1)]
-    chunk_infos = []
-    for c in range(n_chunks):
-        ic = cv.VoxInfo.from_buffer_copy(bytes(info))
-        ic.n_triangles = bounds[c + 1] - bounds[c]
-        chunk_infos.append(ic)
+    # One host-buffer plan (cvx_plan_create_host) is the step: the triangles go up in 2 chunks, the
+    # surface jobs voxelize each chunk as it lands, the solid jobs follow, and each table is copied
+    # down as soon as it is complete.  The link (about 200 GB/s each way here) bounds the step, so
+    # the plan's job is to hide the kernels under the copies; its graph launch also takes the
+    # host's per-call enqueue time out of the step.
+    host_plan = cv.HostPlan([cv.HostJob(info, h_tris, d_tris, out, tab, morton, solid)
+                             for (morton, solid), tab, out in zip(MODES, tables, h_out)], n_chunks=2)
 
     def e2e_step():
-        start = torch.cuda.Event()
-        start.record(stream)
-        copy_stream.wait_event(start)
-        landed = []
-        for c in range(n_chunks):
-            with torch.cuda.stream(copy_stream):
-                d_tris[9 * bounds[c]:9 * bounds[c + 1]].copy_(h_tris[9 * bounds[c]:9 * bounds[c + 1]], non_blocking=True)
-                e = torch.cuda.Event()
-                e.record(copy_stream)
-            landed.append(e)
-        for k, ((morton, solid), tab, out) in enumerate(zip(MODES, tables, h_out)):
+        host_plan.launch()
+
+    def e2e_plain_step():
+        d_tris.copy_(h_tris, non_blocking=True)
+        for (morton, solid), tab, out in zip(MODES, tables, h_out):
             tab.zero_()
-            f = cv.voxelize_solid if solid else cv.voxelize
-            if k == 0:
-                for c in range(n_chunks):
-                    stream.wait_event(landed[c])
-                    f(chunk_infos[c], d_tris[9 * bounds[c]:9 * bounds[c + 1]], tab, morton)
-            else:
-                f(info, d_tris, tab, morton)
-            done = torch.cuda.Event()
-            done.record(stream)
-            copy_stream.wait_event(done)
-            with torch.cuda.stream(copy_stream):
-                out.copy_(tab, non_blocking=True)
-        stream.wait_stream(copy_stream)
+            (cv.voxelize_solid if solid else cv.voxelize)(info, d_tris, tab, morton)
+            out.copy_(tab, non_blocking=True)
+
+    for _ in range(3):
+        e2e_plain_step()
+    torch.cuda.synchronize()
+    plain_times = []
+    for _ in range(min(args.steps, 50)):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e2e_plain_step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_times.append(a.elapsed_time(b))
+    plain_e2e_ms = float(np.mean(plain_times))
 
     for _ in range(3):
         e2e_step()
@@ -436,8 +463,18 @@ def main():
         if not torch.equal(tab.cpu(), out):
             raise RuntimeError(f"e2e table {k} differs from the device-resident result")
     e2e_ms = max_over_ranks(float(np.mean(e2e_times)), world)
+    host_plan.close()
+    # the link's bound on the step: every byte up, then every byte down (no table can leave before
+    # the last triangle has arrived), at the pinned copy rates measured here
+    rates = copy_rates(torch, 256 << 20)
+    copy_bound_ms = (tris.nbytes / (rates["h2d_gbs"] * 1e9) + 4 * W * 4 / (rates["d2h_gbs"] * 1e9)) * 1e3
     e2e = {"value": world * 4 * T / (e2e_ms / 1e3) / 1e6, "unit": "Mtris/s", "ms_per_step": e2e_ms,
-           "h2d_bytes_per_step": int(tris.nbytes), "d2h_bytes_per_step": int(4 * W * 4)}
+           "h2d_bytes_per_step": int(tris.nbytes), "d2h_bytes_per_step": int(4 * W * 4),
+           "path": "cvx_plan_create_host, 2 chunks: surface jobs on each chunk as it lands, solid jobs after, "
+                   "each table read back as soon as it is complete",
+           "copy_bound_ms": copy_bound_ms, "frac_of_copy_bound": copy_bound_ms / e2e_ms, "copy_rates": rates,
+           "plain_calls": {"ms_per_step": plain_e2e_ms, "value": world * 4 * T / (plain_e2e_ms / 1e3) / 1e6,
+                           "note": "upload, 4 calls and 4 read-backs in order on one stream"}}
 
     # ---- the JSON line; the reference CPU baseline and the side measurements on rank 0 -----------
     extras = {}
@@ -448,7 +485,7 @@ def main():
                                    "per step", "gridsize": 512, "triangles": T, "l2": "flushed between steps "
                                    "(512 MiB write, untimed)", "parallelism": f"replicas x{world}"},
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps, "e2e": e2e,
-            "roofline": roofline, "step_as_plan": step_plan}
+            "roofline": roofline, "step_as_plan": step_plan, "step_sequential": step_seq_line}
 
     if rank == 0:
         import oracle

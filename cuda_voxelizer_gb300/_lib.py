@@ -33,6 +33,11 @@ class CvxJob(ctypes.Structure):
                 ("solid", ctypes.c_int32)]
 
 
+class CvxHostJob(ctypes.Structure):
+    _fields_ = [("info", CvxVoxinfo), ("h_triangles", vp), ("d_triangles", vp), ("d_table", vp), ("h_table", vp),
+                ("morton", ctypes.c_int32), ("solid", ctypes.c_int32)]
+
+
 class CvxServerConfig(ctypes.Structure):
     _fields_ = [("memory_budget_bytes", u64), ("max_batch", u32), ("max_inflight", u32)]
 
@@ -71,6 +76,7 @@ SIGNATURES = {
     "cvx_device_status": (c_status, [vp]),
     "cvx_voxelize_batch": (c_status, [ctypes.POINTER(CvxJob), u32, vp]),
     "cvx_plan_create": (c_status, [ctypes.POINTER(CvxJob), u32, u32, ctypes.POINTER(vp)]),
+    "cvx_plan_create_host": (c_status, [ctypes.POINTER(CvxHostJob), u32, u32, ctypes.POINTER(vp)]),
     "cvx_plan_launch": (c_status, [vp, vp]),
     "cvx_plan_destroy": (c_status, [vp]),
     "cvx_server_create": (c_status, [ctypes.POINTER(CvxServerConfig), ctypes.POINTER(vp)]),

@@ -15,11 +15,12 @@ from typing import Sequence
 
 import numpy as np
 
-from ._lib import (CvxError, CvxJob, CvxServerConfig, CvxServerRequest, CvxServerStats, CvxTuning, CvxVoxinfo,
+from ._lib import (CvxError, CvxHostJob, CvxJob, CvxServerConfig, CvxServerRequest, CvxServerStats, CvxTuning, CvxVoxinfo,
                    check, lib)
 
 __all__ = ["VoxInfo", "voxelize", "voxelize_solid", "voxelize_ws", "workspace_size", "create_mesh_bbox_cube",
-           "mesh_bbox", "make_voxinfo", "table_words", "Job", "voxelize_batch", "Plan", "device_status",
+           "mesh_bbox", "make_voxinfo", "table_words", "Job", "voxelize_batch", "Plan", "HostJob", "HostPlan",
+           "device_status",
            "get_tuning", "set_tuning", "CvxError", "voxelize_host", "profile_enable", "profile_collect", "Server",
            "mesh_bbox_device", "voxinfo_from_device", "gather_soup", "transcode", "encode_binvox", "binvox_header",
            "encode_voxel_list"]
@@ -192,6 +193,60 @@ class Plan:
             pass
 
 
+@dataclass
+class HostJob:
+    """One mesh of a host-buffer plan: host triangles in, host table out, with the device buffers
+    the plan copies through.  Host buffers must be page-locked (``tensor.pin_memory()``)."""
+
+    info: VoxInfo
+    h_triangles: object
+    d_triangles: object
+    h_table: object
+    d_table: object
+    morton: bool = False
+    solid: bool = False
+
+
+class HostPlan:
+    """cvx_plan_create_host: the whole round trip -- tables zeroed, triangles up in ``n_chunks``
+    pieces (0: the library's default), surface jobs voxelizing each piece as it lands, solid jobs
+    after the last, each table copied down as soon as it is complete -- as one CUDA graph launch."""
+
+    def __init__(self, jobs: Sequence[HostJob], n_chunks: int = 0):
+        self._jobs = list(jobs)  # keep buffers alive
+        arr = (CvxHostJob * max(1, len(self._jobs)))()
+        for i, j in enumerate(self._jobs):
+            _check_sizes(j.info, j.d_triangles, j.d_table)
+            if j.info.n_triangles and _host_nbytes(j.h_triangles) < 36 * j.info.n_triangles:
+                raise ValueError(f"job {i}: h_triangles holds fewer than {9 * j.info.n_triangles} floats")
+            if _host_nbytes(j.h_table) < 4 * table_words(j.info):
+                raise ValueError(f"job {i}: h_table holds fewer than {4 * table_words(j.info)} bytes")
+            arr[i].info = j.info
+            arr[i].h_triangles = _host_ptr(j.h_triangles, False) if j.info.n_triangles else 0
+            arr[i].d_triangles = _ptr(j.d_triangles)
+            arr[i].d_table = _ptr(j.d_table)
+            arr[i].h_table = _host_ptr(j.h_table, True)
+            arr[i].morton = int(bool(j.morton))
+            arr[i].solid = int(bool(j.solid))
+        h = ctypes.c_void_p()
+        check(lib.cvx_plan_create_host(arr, len(self._jobs), int(n_chunks), ctypes.byref(h)), "cvx_plan_create_host")
+        self._h = h
+
+    def launch(self, stream=None) -> None:
+        check(lib.cvx_plan_launch(self._h, _stream(stream)), "cvx_plan_launch")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.cvx_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def profile_enable(on: bool = True) -> None:
     """Record per-kernel CUDA events for the calls of this thread (see profile_collect)."""
     check(lib.cvx_profile_enable(int(bool(on))), "cvx_profile_enable")
@@ -233,7 +288,7 @@ def _host_ptr(x, writable: bool) -> int:
     server's copies overlap with other batches)."""
     if hasattr(x, "data_ptr"):
         if x.is_cuda:
-            raise ValueError("server requests take host buffers")
+            raise ValueError("expected a host buffer, got a CUDA tensor")
         if not x.is_contiguous():
             raise ValueError("host buffers must be contiguous")
         return int(x.data_ptr())

@@ -27,6 +27,7 @@ static_assert(sizeof(cvx_voxinfo) == 64, "cvx_voxinfo must match the reference v
 static_assert(offsetof(cvx_voxinfo, gridsize) == 24, "voxinfo.gridsize offset");
 static_assert(offsetof(cvx_voxinfo, n_triangles) == 40, "voxinfo.n_triangles offset");
 static_assert(offsetof(cvx_voxinfo, unit) == 48, "voxinfo.unit offset");
+static_assert(sizeof(cvx_host_job) == 104, "cvx_host_job layout (the Python binding mirrors it)");
 
 namespace {
 
@@ -693,6 +694,35 @@ struct cvx_plan {
 // latency-bound cooperative kernel runs beside another lane's classify kernel).
 constexpr int kPlanSurfaceLanes = 2;
 
+// One group's launches on a capturing stream, as Runner::run issues them but with the group's job
+// array (when it has more than one job) already resident at `jobs_dev`.
+static cudaError_t capture_group(const Group& g, bool solid, bool resolve, void* rec, uint64_t cap, JobDesc* jobs_dev,
+                          const DevState& dev, cudaStream_t s) {
+	const RecLayout l0 = rec_layout(cap, 0);
+	LaunchDesc L;
+	std::memset(&L, 0, sizeof(L));
+	L.n_jobs = (uint32_t)g.jobs.size();
+	L.n_tiles = g.tiles;
+	L.n_units = g.units;
+	L.n_mwords = g.mwords;
+	L.n_mbricks = g.mbricks;
+	L.n_mslabs = g.mslabs;
+	L.slab_smem = g.slab_smem;
+	L.scr.ctr = reinterpret_cast<Counters*>(rec);
+	L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(rec) + l0.big);
+	L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(rec) + l0.mid);
+	L.scr.cap = (uint32_t)cap;
+	if (g.jobs.size() == 1)
+		L.single = g.jobs[0];
+	else
+		L.jobs = jobs_dev;
+	if (resolve) return launch_solid(L, dev.tune, dev.cols_grid, s, kSolidResolve, nullptr);
+	const cudaError_t e = cudaMemsetAsync(rec, 0, kCountersResetBytes, s);
+	if (e != cudaSuccess) return e;
+	return solid ? launch_solid(L, dev.tune, dev.cols_grid, s, kSolidToggles, nullptr)
+	             : launch_surface(L, dev.tune, dev.rows_grid, s, nullptr);
+}
+
 cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out) {
 	if (!out) return fail(CVX_ERR_INVALID_VALUE, "out is null");
 	*out = nullptr;
@@ -847,7 +877,6 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 	for (size_t li = 0; li < lanes.size() && cst == CVX_OK; li++) {
 		Lane& l = lanes[li];
 		void* rec = p->recs[li];
-		const RecLayout l0 = rec_layout(l.cap, 0);
 		if ((fork && cudaStreamWaitEvent(l.stream, fork_ev, 0) != cudaSuccess) ||
 		    cudaMemsetAsync(rec, 0, sizeof(Counters), l.stream) != cudaSuccess) {
 			cst = cuda_fail(cudaGetLastError(), "capture lane");
@@ -855,36 +884,10 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		}
 		size_t used = l.job_off;
 		for (size_t gi = 0; gi < l.groups.size() && cst == CVX_OK; gi++) {
-			Group& g = l.groups[gi];
+			const Group& g = l.groups[gi];
 			const bool resolve = l.solid && gi + 1 == l.groups.size();
-			LaunchDesc L;
-			std::memset(&L, 0, sizeof(L));
-			L.n_jobs = (uint32_t)g.jobs.size();
-			L.n_tiles = g.tiles;
-			L.n_units = g.units;
-			L.n_mwords = g.mwords;
-			L.n_mbricks = g.mbricks;
-			L.n_mslabs = g.mslabs;
-			L.slab_smem = g.slab_smem;
-			L.scr.ctr = reinterpret_cast<Counters*>(rec);
-			L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(rec) + l0.big);
-			L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(rec) + l0.mid);
-			L.scr.cap = (uint32_t)l.cap;
-			if (g.jobs.size() == 1) {
-				L.single = g.jobs[0];
-			} else {
-				L.jobs = p->job_area + used;
-				used += g.jobs.size();
-			}
-			cudaError_t e = cudaSuccess;
-			if (resolve) {
-				e = launch_solid(L, dev.tune, dev.cols_grid, l.stream, kSolidResolve, nullptr);
-			} else {
-				e = cudaMemsetAsync(rec, 0, kCountersResetBytes, l.stream);
-				if (e == cudaSuccess)
-					e = l.solid ? launch_solid(L, dev.tune, dev.cols_grid, l.stream, kSolidToggles, nullptr)
-					            : launch_surface(L, dev.tune, dev.rows_grid, l.stream, nullptr);
-			}
+			const cudaError_t e = capture_group(g, l.solid, resolve, rec, l.cap, p->job_area + used, dev, l.stream);
+			if (g.jobs.size() > 1) used += g.jobs.size();
 			if (e != cudaSuccess) cst = cuda_fail(e, "capture launch");
 		}
 		if (cst == CVX_OK && fork &&
@@ -894,6 +897,324 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 	cudaGraph_t graph = nullptr;
 	cudaError_t ee = cudaStreamEndCapture(cs, &graph);
 	drop_streams();
+	if (cst != CVX_OK) {
+		if (graph) cudaGraphDestroy(graph);
+		return bail(cst);
+	}
+	if (ee != cudaSuccess) return bail(cuda_fail(ee, "end capture"));
+	p->graph = graph;
+	if (cudaGraphInstantiate(&p->exec, graph, 0) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "instantiate"));
+	*out = p;
+	return CVX_OK;
+}
+
+// ---- host-buffer plans: upload, voxelize and read back as one graph -------------------------------
+
+namespace {
+
+constexpr uint32_t kHostPlanDefaultChunks = 2;
+constexpr uint32_t kHostPlanMaxChunks = 64;
+
+bool page_locked(const void* p) {
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeHost;
+}
+
+// One mesh's triangles on their way up: the host source, the device destination and the chunk
+// bounds (in triangles; interior bounds on whole 256-triangle tiles, so every chunk but the last
+// starts 16-byte aligned when the buffer does and keeps the classify kernels' bulk tile copy).
+struct Upload {
+	const float* h = nullptr;
+	const float* d = nullptr;
+	uint64_t n = 0;
+	std::vector<uint64_t> bounds;
+};
+
+// One step of a host plan's compute stream, in issue order.
+struct HostStep {
+	enum Kind { kWait, kLaunch, kResolve, kFinal } kind;
+	uint32_t u = 0, c = 0;  // kWait: upload u's chunk c has landed
+	uint32_t job = 0;       // kFinal: the caller's job whose table is now complete
+	bool solid = false;
+	Group g;                // kLaunch / kResolve
+	size_t slot = 0;        // first JobDesc slot of g's job array (groups of more than one job)
+};
+
+}  // namespace
+
+// A host-buffer plan is the round trip of plain calls on host memory -- copy the triangles up,
+// voxelize, copy the tables down -- arranged for a link that is slower than the kernels: the copies
+// bound it, so the plan keeps the link busy.  Meshes go up one after another, each in chunks, on a
+// copy stream; one compute stream runs the surface jobs on each chunk as soon as it lands (exact: a
+// surface table is the OR of its chunks' bits), so they complete with the last chunk; then each
+// solid table in turn over the whole mesh.  Tables are completed one at a time so that a read-back
+// stream can copy each down while the next is still being computed.
+cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint32_t n_chunks, cvx_plan** out) {
+	if (!out) return fail(CVX_ERR_INVALID_VALUE, "out is null");
+	*out = nullptr;
+	if (n_jobs && !jobs) return fail(CVX_ERR_INVALID_VALUE, "jobs is null");
+	if (n_chunks == 0) n_chunks = kHostPlanDefaultChunks;
+	if (n_chunks > kHostPlanMaxChunks) return fail(CVX_ERR_INVALID_VALUE, "n_chunks above %u", kHostPlanMaxChunks);
+	for (uint32_t i = 0; i < n_jobs; i++) {
+		const cvx_host_job& J = jobs[i];
+		cvx_status st = validate(&J.info, J.d_triangles, J.d_table, J.morton);
+		if (st != CVX_OK) return fail(st, "job %u: %s", i, g_msg.c_str());
+		if (!J.h_table) return fail(CVX_ERR_INVALID_VALUE, "job %u: h_table is null", i);
+		if (J.info.n_triangles && !J.h_triangles) return fail(CVX_ERR_INVALID_VALUE, "job %u: h_triangles is null", i);
+	}
+	DevState dev;
+	cvx_status st = dev_state(dev);
+	if (st != CVX_OK) return st;
+	std::vector<Upload> ups;
+	std::vector<int> up_of(n_jobs, -1);
+	for (uint32_t i = 0; i < n_jobs; i++) {
+		const cvx_host_job& J = jobs[i];
+		if (!page_locked(J.h_table)) return fail(CVX_ERR_INVALID_VALUE, "job %u: h_table is not page-locked host memory", i);
+		if (J.info.n_triangles == 0) continue;
+		if (!page_locked(J.h_triangles))
+			return fail(CVX_ERR_INVALID_VALUE, "job %u: h_triangles is not page-locked host memory", i);
+		int u = -1;
+		for (size_t k = 0; k < ups.size(); k++) {
+			if (ups[k].d != J.d_triangles) continue;
+			if (ups[k].h != J.h_triangles || ups[k].n != J.info.n_triangles)
+				return fail(CVX_ERR_INVALID_VALUE, "job %u: d_triangles receives a different upload in another job", i);
+			u = (int)k;
+		}
+		if (u < 0) {
+			Upload up;
+			up.h = J.h_triangles;
+			up.d = J.d_triangles;
+			up.n = J.info.n_triangles;
+			up.bounds.resize(n_chunks + 1);
+			for (uint32_t c = 0; c < n_chunks; c++) up.bounds[c] = up.n * c / n_chunks / kTile * kTile;
+			up.bounds[n_chunks] = up.n;
+			u = (int)ups.size();
+			ups.push_back(std::move(up));
+		}
+		up_of[i] = u;
+	}
+
+	cvx_plan* p = new cvx_plan();
+	auto bail = [&](cvx_status s2) {
+		cvx_plan_destroy(p);
+		return s2;
+	};
+	// Flip tables of the solid jobs.
+	std::vector<uint32_t*> flips(n_jobs, nullptr);
+	{
+		std::vector<JobDesc> full;
+		std::vector<uint32_t> idx;
+		for (uint32_t i = 0; i < n_jobs; i++)
+			if (jobs[i].solid && up_of[i] >= 0) {
+				full.push_back(make_job(jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton, 1));
+				idx.push_back(i);
+			}
+		uint64_t flip_total = 0;
+		for (const JobDesc& j : full) flip_total += flip_bytes_of(j);
+		if (flip_total) {
+			if (cudaMalloc((void**)&p->flips, flip_total) != cudaSuccess) {
+				cudaGetLastError();
+				return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan flip tables"));
+			}
+			if (cudaMemset(p->flips, 0, flip_total) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "memset"));
+			assign_flips(full, p->flips);
+			for (size_t k = 0; k < idx.size(); k++) flips[idx[k]] = full[k].flips;
+		}
+	}
+	auto job_of = [&](uint32_t i, uint64_t b0, uint64_t b1) {
+		cvx_voxinfo v = jobs[i].info;
+		v.n_triangles = b1 - b0;
+		JobDesc j = make_job(v, jobs[i].d_triangles + 9 * b0, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
+		j.flips = flips[i];
+		return j;
+	};
+	// The compute stream's steps.  Jobs without triangles are complete once cleared.
+	std::vector<HostStep> steps;
+	for (uint32_t i = 0; i < n_jobs; i++)
+		if (up_of[i] < 0) {
+			HostStep f;
+			f.kind = HostStep::kFinal;
+			f.job = i;
+			steps.push_back(std::move(f));
+		}
+	uint64_t cap = 1;
+	size_t slots = 0;
+	auto add_groups = [&](std::vector<JobDesc>& part, bool solid) {
+		if (part.empty()) return;
+		for (Group& g : make_groups(part, solid)) {
+			HostStep st;
+			st.kind = HostStep::kLaunch;
+			st.solid = solid;
+			cap = std::max<uint64_t>(cap, g.tris);
+			st.slot = slots;
+			if (g.jobs.size() > 1) slots += g.jobs.size();
+			st.g = std::move(g);
+			steps.push_back(std::move(st));
+		}
+		part.clear();
+	};
+	for (uint32_t u = 0; u < (uint32_t)ups.size(); u++) {
+		std::vector<uint32_t> mine;
+		for (uint32_t i = 0; i < n_jobs; i++)
+			if (up_of[i] == (int)u) mine.push_back(i);
+		for (uint32_t c = 0; c < n_chunks; c++) {
+			const uint64_t b0 = ups[u].bounds[c], b1 = ups[u].bounds[c + 1];
+			if (b1 == b0) continue;
+			HostStep w;
+			w.kind = HostStep::kWait;
+			w.u = u;
+			w.c = c;
+			steps.push_back(std::move(w));
+			const bool last = b1 == ups[u].n;
+			std::vector<JobDesc> part;
+			if (!last) {
+				for (uint32_t i : mine)
+					if (!jobs[i].solid) part.push_back(job_of(i, b0, b1));
+				add_groups(part, false);
+				continue;
+			}
+			// The last chunk one surface job at a time, each table read back as soon as it is done:
+			// the link starts on the first table after a fraction of the chunk's work.
+			for (uint32_t i : mine)
+				if (!jobs[i].solid) {
+					part.push_back(job_of(i, b0, b1));
+					add_groups(part, false);
+					HostStep f;
+					f.kind = HostStep::kFinal;
+					f.job = i;
+					steps.push_back(std::move(f));
+				}
+			// The solid tables one at a time over the whole mesh: toggles, resolve, read back.  (Per
+			// chunk they would cost a persistent column launch each, which the upload cannot hide.)
+			for (uint32_t i : mine)
+				if (jobs[i].solid) {
+					part.push_back(job_of(i, 0, ups[u].n));
+					add_groups(part, true);
+					HostStep r;
+					r.kind = HostStep::kResolve;
+					r.solid = true;
+					r.g = resolve_group(std::vector<JobDesc>{job_of(i, 0, ups[u].n)});
+					r.slot = slots;
+					steps.push_back(std::move(r));
+					HostStep f;
+					f.kind = HostStep::kFinal;
+					f.job = i;
+					steps.push_back(std::move(f));
+				}
+		}
+	}
+	if (slots) {
+		if (cudaMalloc((void**)&p->job_area, slots * sizeof(JobDesc)) != cudaSuccess) {
+			cudaGetLastError();
+			return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan job arrays"));
+		}
+		std::vector<JobDesc> all;
+		for (const HostStep& st : steps)
+			if (st.kind == HostStep::kLaunch && st.g.jobs.size() > 1) all.insert(all.end(), st.g.jobs.begin(), st.g.jobs.end());
+		if (cudaMemcpy(p->job_area, all.data(), all.size() * sizeof(JobDesc), cudaMemcpyHostToDevice) != cudaSuccess)
+			return bail(cuda_fail(cudaGetLastError(), "job upload"));
+	}
+	void* rec = nullptr;
+	if (cudaMalloc(&rec, rec_layout(cap, 0).end) != cudaSuccess) {
+		cudaGetLastError();
+		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
+	}
+	p->recs.push_back(rec);
+
+	// The capture: compute on the origin stream, uploads on cp, read-backs on rb.
+	cudaStream_t cs = nullptr, cp = nullptr, rb = nullptr;
+	cudaEvent_t fork_ev = nullptr, copied = nullptr, read = nullptr;
+	std::vector<std::vector<cudaEvent_t>> landed(ups.size(), std::vector<cudaEvent_t>(n_chunks, nullptr));
+	std::vector<cudaEvent_t> final_ev(n_jobs, nullptr);
+	cvx_status cst = CVX_OK;
+	auto mk_stream = [&](cudaStream_t* st) {
+		if (cst == CVX_OK && cudaStreamCreateWithFlags(st, cudaStreamNonBlocking) != cudaSuccess) {
+			*st = nullptr;
+			cst = cuda_fail(cudaGetLastError(), "stream");
+		}
+	};
+	auto mk_event = [&](cudaEvent_t* e) {
+		if (cst == CVX_OK && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+			*e = nullptr;
+			cst = cuda_fail(cudaGetLastError(), "event");
+		}
+	};
+	mk_stream(&cs);
+	mk_stream(&cp);
+	mk_stream(&rb);
+	mk_event(&fork_ev);
+	mk_event(&copied);
+	mk_event(&read);
+	for (auto& v : landed)
+		for (cudaEvent_t& e : v) mk_event(&e);
+	for (cudaEvent_t& e : final_ev) mk_event(&e);
+	auto drop = [&]() {
+		for (auto& v : landed)
+			for (cudaEvent_t e : v)
+				if (e) cudaEventDestroy(e);
+		for (cudaEvent_t e : final_ev)
+			if (e) cudaEventDestroy(e);
+		for (cudaStream_t st : {cs, cp, rb})
+			if (st) cudaStreamDestroy(st);
+		for (cudaEvent_t e : {fork_ev, copied, read})
+			if (e) cudaEventDestroy(e);
+	};
+	if (cst != CVX_OK) {
+		drop();
+		return bail(cst);
+	}
+	if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+		drop();
+		return bail(cuda_fail(cudaGetLastError(), "begin capture"));
+	}
+	auto ck = [&](cudaError_t e, const char* what) {
+		if (cst == CVX_OK && e != cudaSuccess) cst = cuda_fail(e, what);
+	};
+	ck(cudaEventRecord(fork_ev, cs), "capture fork");
+	ck(cudaStreamWaitEvent(cp, fork_ev, 0), "capture fork");
+	ck(cudaStreamWaitEvent(rb, fork_ev, 0), "capture fork");
+	for (size_t u = 0; u < ups.size() && cst == CVX_OK; u++)
+		for (uint32_t c = 0; c < n_chunks && cst == CVX_OK; c++) {
+			const uint64_t b0 = ups[u].bounds[c], b1 = ups[u].bounds[c + 1];
+			if (b1 == b0) continue;
+			ck(cudaMemcpyAsync(const_cast<float*>(ups[u].d) + 9 * b0, ups[u].h + 9 * b0, (b1 - b0) * 36,
+			                   cudaMemcpyHostToDevice, cp),
+			   "capture upload");
+			ck(cudaEventRecord(landed[u][c], cp), "capture upload");
+		}
+	ck(cudaEventRecord(copied, cp), "capture upload");
+	for (uint32_t i = 0; i < n_jobs; i++) ck(cudaMemsetAsync(jobs[i].d_table, 0, words_of(jobs[i].info) * 4, cs), "capture clear");
+	ck(cudaMemsetAsync(rec, 0, sizeof(Counters), cs), "capture clear");
+	for (const HostStep& st : steps) {
+		if (cst != CVX_OK) break;
+		switch (st.kind) {
+		case HostStep::kWait:
+			ck(cudaStreamWaitEvent(cs, landed[st.u][st.c], 0), "capture wait");
+			break;
+		case HostStep::kLaunch:
+		case HostStep::kResolve:
+			ck(capture_group(st.g, st.solid, st.kind == HostStep::kResolve, rec, cap, p->job_area + st.slot, dev, cs),
+			   "capture launch");
+			break;
+		case HostStep::kFinal: {
+			const cvx_host_job& J = jobs[st.job];
+			ck(cudaEventRecord(final_ev[st.job], cs), "capture read-back");
+			ck(cudaStreamWaitEvent(rb, final_ev[st.job], 0), "capture read-back");
+			ck(cudaMemcpyAsync(J.h_table, J.d_table, words_of(J.info) * 4, cudaMemcpyDeviceToHost, rb), "capture read-back");
+			break;
+		}
+		}
+	}
+	ck(cudaEventRecord(read, rb), "capture join");
+	ck(cudaStreamWaitEvent(cs, read, 0), "capture join");
+	ck(cudaStreamWaitEvent(cs, copied, 0), "capture join");
+	cudaGraph_t graph = nullptr;
+	const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+	drop();
 	if (cst != CVX_OK) {
 		if (graph) cudaGraphDestroy(graph);
 		return bail(cst);
@@ -930,7 +1251,6 @@ cvx_status cvx_profile_enable(int on) {
 
 int cvx_profile_collect(const char** names, float* ms, int max_entries) {
 	int n = 0;
-	const char* pending = nullptr;
 	cudaEvent_t prev = nullptr;
 	for (const Mark& m : t_marks) {
 		if (cudaEventSynchronize(m.ev) != cudaSuccess) break;
@@ -941,7 +1261,6 @@ int cvx_profile_collect(const char** names, float* ms, int max_entries) {
 			if (ms) ms[n] = t;
 			n++;
 		}
-		(void)pending;
 		prev = m.ev;
 	}
 	for (const Mark& m : t_marks) cudaEventDestroy(m.ev);

@@ -133,6 +133,28 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 cvx_status cvx_plan_launch(cvx_plan* plan, cvx_stream_t stream);
 cvx_status cvx_plan_destroy(cvx_plan* plan);
 
+/* Host-buffer plans: the reference's round trip (src/main.cpp:209-222 hands voxelize host-visible
+ * triangles and table) as one graph.  Each launch copies every job's triangles from h_triangles into
+ * d_triangles, zeroes d_table, voxelizes, and copies d_table into h_table; the tables are
+ * bit-identical to plain calls.  Meshes go up in job order, each in n_chunks pieces (0 = 2, at most
+ * 64); the surface jobs voxelize each piece as soon as it lands, the solid jobs follow the mesh's
+ * last piece, and each table is copied down as soon as it is complete, so the kernels run under
+ * the copies and the link stays busy.  Jobs that share
+ * d_triangles must share h_triangles and n_triangles (one upload serves them); different uploads
+ * and different tables must not overlap.  Host buffers must be page-locked (cudaHostAlloc or
+ * cudaHostRegister).  Launch with cvx_plan_launch; the host tables are complete when the launch's
+ * stream reaches the point after it.  Destroy with cvx_plan_destroy. */
+typedef struct cvx_host_job {
+	cvx_voxinfo info;
+	const float* h_triangles; /* host source, n_triangles * 9 floats */
+	float* d_triangles;       /* device copy of them, written by the plan */
+	uint32_t* d_table;        /* device table (zeroed by the plan) */
+	uint32_t* h_table;        /* host destination of the table */
+	int32_t morton;
+	int32_t solid;
+} cvx_host_job;
+cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint32_t n_chunks, cvx_plan** out);
+
 /* ---- serving: requests admitted by device memory and batched continuously --------------------
  * No counterpart in the reference (src/main.cpp voxelizes one mesh per process).  A server owns
  * one device arena of memory_budget_bytes (allocated at creation, nothing else is allocated while

@@ -117,3 +117,31 @@ def test_server_request_struct_layout():
     assert ctypes.sizeof(R) == 64 + 8 + 8 + 8 + 4 + 4
     assert R.h_triangles.offset == 64 and R.d_triangles.offset == 72 and R.h_table.offset == 80
     assert R.solid.offset == 92
+
+
+def test_host_job_struct_layout():
+    J = _lib.CvxHostJob
+    assert ctypes.sizeof(J) == 104  # static_assert in the library
+    assert (J.h_triangles.offset, J.d_triangles.offset, J.d_table.offset, J.h_table.offset) == (64, 72, 80, 88)
+    assert J.morton.offset == 96 and J.solid.offset == 100
+
+
+def test_host_plan_validation_answers_without_a_gpu():
+    info = _info()
+    info.n_triangles = 10
+    h = ctypes.c_void_p()
+    job = _lib.CvxHostJob()
+    job.info = info
+    job.h_triangles, job.d_triangles, job.d_table, job.h_table = 16, 32, 48, 64
+    assert _lib.lib.cvx_plan_create_host(ctypes.byref(job), 1, 0, None) == 1  # out is null
+    assert _lib.lib.cvx_plan_create_host(None, 1, 0, ctypes.byref(h)) == 1  # jobs is null
+    assert _lib.lib.cvx_plan_create_host(ctypes.byref(job), 1, 65, ctypes.byref(h)) == 1
+    assert b"n_chunks" in _lib.lib.cvx_last_error_message()
+    for field in ("h_table", "h_triangles", "d_table", "d_triangles"):
+        bad = _lib.CvxHostJob.from_buffer_copy(bytes(job))
+        setattr(bad, field, None)
+        assert _lib.lib.cvx_plan_create_host(ctypes.byref(bad), 1, 0, ctypes.byref(h)) == 1
+        assert not h.value
+    job.morton = 1
+    job.info.gridsize[1] = 32  # Morton order needs a cubic power-of-two grid
+    assert _lib.lib.cvx_plan_create_host(ctypes.byref(job), 1, 0, ctypes.byref(h)) != 0
