@@ -488,9 +488,10 @@ struct cvx_server {
 extern "C" {
 
 cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out) {
-	if (!cfg || !out || cfg->memory_budget_bytes < (1u << 20) || cfg->max_batch == 0 || cfg->max_inflight == 0 ||
-	    cfg->max_inflight > 64) {
-		cvx::set_message("cvx_server_create: need a budget of at least 1 MiB, max_batch > 0, 0 < max_inflight <= 64");
+	if (!cfg || !out || cfg->memory_budget_bytes < (1u << 20) || cfg->max_batch == 0 || cfg->max_batch > 65536 ||
+	    cfg->max_inflight == 0 || cfg->max_inflight > 64) {
+		cvx::set_message("cvx_server_create: need a budget of at least 1 MiB, 0 < max_batch <= 65536, "
+		                 "0 < max_inflight <= 64");
 		return CVX_ERR_INVALID_VALUE;
 	}
 	auto s = std::make_unique<cvx_server>();
@@ -504,16 +505,30 @@ cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out) {
 		cvx::set_message("cvx_server_create: cannot allocate the memory budget");
 		return CVX_ERR_OUT_OF_MEMORY;
 	}
+	// Each slot's pinned host buffers are allocated here, not while serving: a pinned allocation is
+	// a slow driver call that holds up the other streams' launches.  The clear list is exact
+	// (a table and a flip table per request); the job staging covers every batch of max_batch
+	// jobs that no launch has to split (over 2^24 triangles), and only grows for one that does.
+	const size_t staging_bytes = std::max<size_t>((4 * (size_t)cfg->max_batch + 64) * sizeof(cvx::JobDesc), (size_t)64 << 10);
 	for (uint32_t i = 0; i < cfg->max_inflight; i++) {
 		auto sl = std::make_unique<Slot>();
 		sl->server = s.get();
-		if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess) {
+		bool ok = cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) == cudaSuccess;
+		if (ok) ok = cudaMallocHost(&sl->staging, staging_bytes) == cudaSuccess;
+		if (ok) sl->staging_bytes = staging_bytes;
+		if (ok) ok = cudaMallocHost((void**)&sl->h_clears, 2 * (size_t)cfg->max_batch * sizeof(cvx::ClearRange)) == cudaSuccess;
+		if (ok) sl->h_clears_n = 2 * (size_t)cfg->max_batch;
+		s->slots.push_back(std::move(sl));
+		if (!ok) {
 			cudaGetLastError();
-			for (auto& o : s->slots) cudaStreamDestroy(o->stream);
-			cvx::set_message("cvx_server_create: cannot create streams");
+			for (auto& o : s->slots) {
+				if (o->stream) cudaStreamDestroy(o->stream);
+				if (o->staging) cudaFreeHost(o->staging);
+				if (o->h_clears) cudaFreeHost(o->h_clears);
+			}
+			cvx::set_message("cvx_server_create: cannot create streams or pinned staging");
 			return CVX_ERR_CUDA;
 		}
-		s->slots.push_back(std::move(sl));
 	}
 	cvx_server* p = s.release();
 	p->worker = std::thread([p] { p->run(); });

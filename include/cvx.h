@@ -169,7 +169,7 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 typedef struct cvx_server cvx_server;
 typedef struct cvx_server_config {
 	uint64_t memory_budget_bytes;
-	uint32_t max_batch;     /* requests per launch sequence */
+	uint32_t max_batch;     /* requests per launch sequence, 1 .. 65536 */
 	uint32_t max_inflight;  /* batches on the GPU at once (one stream each) */
 } cvx_server_config;
 typedef struct cvx_server_request {

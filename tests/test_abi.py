@@ -104,7 +104,8 @@ def test_mesh_bbox_host():
 
 def test_server_config_validation_answers_without_a_gpu():
     h = ctypes.c_void_p()
-    for budget, batch, inflight in ((0, 8, 2), (64 << 20, 0, 2), (64 << 20, 8, 0), (64 << 20, 8, 65)):
+    for budget, batch, inflight in ((0, 8, 2), (64 << 20, 0, 2), (64 << 20, 65537, 2), (64 << 20, 8, 0),
+                                    (64 << 20, 8, 65)):
         cfg = _lib.CvxServerConfig(budget, batch, inflight)
         assert _lib.lib.cvx_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
     assert b"budget" in _lib.lib.cvx_last_error_message()
