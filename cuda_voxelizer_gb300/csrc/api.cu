@@ -221,6 +221,8 @@ JobDesc make_job(const cvx_voxinfo& v, const float* tris, uint32_t* table, int m
 		j.grid[i] = v.gridsize[i];
 	}
 	j.flags = (morton ? JOB_MORTON : 0u) | (solid ? JOB_SOLID : 0u);
+	const uint64_t voxels = (uint64_t)v.gridsize[0] * v.gridsize[1] * v.gridsize[2];
+	if (morton ? v.gridsize[0] <= 1024 : voxels <= (1ull << 32)) j.flags |= JOB_NARROW;
 	return j;
 }
 

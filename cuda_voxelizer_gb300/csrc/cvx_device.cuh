@@ -60,7 +60,10 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 // ------------------------------------------------------------------------------------------------
 // Job and launch descriptors.
 
-enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u };
+// JOB_NARROW: every voxel index of the job fits 32 bits (linear: gx*gy*gz <= 2^32; Morton: a cubic
+// grid of at most 1024), so the surface writes compute indices and Morton codes in 32-bit
+// arithmetic.  Set by the host; a hint only (the 64-bit path gives the same words).
+enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u };
 
 // One mesh voxelization.  Plain data, uploaded as an array for batches or passed by value for a
 // single mesh.
@@ -73,7 +76,7 @@ struct JobDesc {
 	float unit[3];
 	float inv_unit[3];     // 1.0f / unit, correctly rounded (host); only used for the exactly checked div_trunc
 	uint32_t grid[3];
-	uint32_t flags;        // JOB_MORTON | JOB_SOLID
+	uint32_t flags;        // JOB_MORTON | JOB_SOLID | JOB_NARROW
 	uint32_t tile_begin;   // first triangle tile of this job in the launch's tile space
 	uint32_t unit_begin;   // solid: first resolve unit of this job in the launch's unit space
 	uint64_t mword_begin;  // solid Morton, g < 32: first Morton word in the launch's word space
@@ -182,6 +185,21 @@ __device__ __forceinline__ uint64_t spread3(uint32_t v) {
 	x = (x | (x << 2)) & 0x249249249249ull;
 	return x;
 }
+// spread3 of v < 1024 in 32-bit arithmetic (bit i of v to bit 3i, i < 10).
+__device__ __forceinline__ uint32_t spread3_narrow(uint32_t v) {
+	uint32_t x = v & 0x3FFu;
+	x = (x | (x << 16)) & 0xFF0000FFu;
+	x = (x | (x << 8)) & 0x0300F00Fu;
+	x = (x | (x << 4)) & 0x030C30C3u;
+	x = (x | (x << 2)) & 0x09249249u;
+	return x;
+}
+// spread3 in the code type of a write path: uint32_t (JOB_NARROW) or uint64_t.
+template <class C>
+__device__ __forceinline__ C spread3_t(uint32_t v) {
+	if constexpr (sizeof(C) == 4) return spread3_narrow(v);
+	else return spread3(v);
+}
 __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
 	return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
 }
@@ -237,9 +255,10 @@ __device__ __forceinline__ uint32_t span_mask(uint32_t a, uint32_t b) {
 }
 
 // OR bits [lo, hi] of the linear bit stream into the table, one atomic per word.
-__device__ __forceinline__ void or_span(uint32_t* table, uint64_t lo, uint64_t hi) {
-	uint64_t w0 = lo >> 5, w1 = hi >> 5;
-	for (uint64_t w = w0; w <= w1; w++) {
+template <class C = uint64_t>
+__device__ __forceinline__ void or_span(uint32_t* table, C lo, C hi) {
+	C w0 = lo >> 5, w1 = hi >> 5;
+	for (C w = w0; w <= w1; w++) {
 		uint32_t a = (w == w0) ? (uint32_t)(lo & 31u) : 0u;
 		uint32_t b = (w == w1) ? (uint32_t)(hi & 31u) : 31u;
 		atomicOr(table + w, span_mask(a, b));
@@ -253,22 +272,29 @@ constexpr uint64_t kMortonX1 = 1ull, kMortonX4 = 64ull;
 __device__ __forceinline__ uint64_t morton_x_add(uint64_t xd, uint64_t step) {
 	return ((xd | ~kMortonXMask) + step) & kMortonXMask;
 }
+// The same in the code type of a write path (the 32-bit mask covers x < 1024).
+template <class C>
+__device__ __forceinline__ C morton_x_add_t(C xd, C step) {
+	if constexpr (sizeof(C) == 4) return ((xd | ~0x09249249u) + step) & 0x09249249u;
+	else return morton_x_add(xd, step);
+}
 
 // OR the Morton-ordered bits of row (y, z), x in [xl, xh], one atomic per touched word.  Within a
 // Morton word (32 consecutive codes) x varies in its two low bits only: codes of x = 4k..4k+3 sit at
 // offsets {0, 1, 8, 9} from the code of x = 4k, i.e. MSB-first bits 31, 30, 23, 22 shifted right
 // by that code's offset in its word.
+template <class C = uint64_t>
 __device__ __forceinline__ void or_span_morton(uint32_t* table, int xl, int xh, uint32_t y, uint32_t z) {
-	const uint64_t yz = (spread3(y) << 1) | (spread3(z) << 2);
+	const C yz = (spread3_t<C>(y) << 1) | (spread3_t<C>(z) << 2);
 	const int k1 = xh >> 2;
-	uint64_t xd = spread3((uint32_t)(xl & ~3));
+	C xd = spread3_t<C>((uint32_t)(xl & ~3));
 	for (int k = xl >> 2; k <= k1; k++) {
-		const uint64_t code = xd | yz;
+		const C code = xd | yz;
 		const int j0 = max(xl - (k << 2), 0), j1 = min(xh - (k << 2), 3);
 		const uint32_t n = (0xFu << j0) & (0xFu >> (3 - j1));  // x offsets j0..j1 of the group
 		const uint32_t m = ((n & 1u) << 31) | ((n & 2u) << 29) | ((n & 4u) << 21) | ((n & 8u) << 19);
 		atomicOr(table + (code >> 5), m >> (uint32_t)(code & 31u));
-		xd = morton_x_add(xd, kMortonX4);
+		xd = morton_x_add_t<C>(xd, (C)kMortonX4);
 	}
 }
 

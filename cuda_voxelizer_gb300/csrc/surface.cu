@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 	uint32_t* table = J.table;
 	const uint64_t n = J.n_tri;
 	const bool morton = (J.flags & JOB_MORTON) != 0;
+	const bool narrow = (J.flags & JOB_NARROW) != 0;
 	const float bmin[3] = {J.bmin[0], J.bmin[1], J.bmin[2]};
 	const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
 	const float inv[3] = {J.inv_unit[0], J.inv_unit[1], J.inv_unit[2]};
@@ -240,12 +241,12 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 			// src/voxelize.cu:136-183: every voxel of the row (at most 16), as a pass mask
 			uint32_t pm = 0;
 			for (int i = 0; i <= S.bx1 - S.bx0; i++) pm |= (uint32_t)voxel_pass<P>(S, K, unit[0], S.bx0 + i) << i;
-			if (pm) write_row_mask(table, morton, grid, y, z, S.bx0, pm);
+			if (pm) write_row_mask(table, morton, narrow, grid, y, z, S.bx0, pm);
 		} else {
 			RowDirs D;
 			row_dirs(S, unit[0], D);
 			int xl, xh;
-			if (row_interval<P>(S, D, K, unit[0], xl, xh)) write_row(table, morton, grid, y, z, xl, xh);
+			if (row_interval<P>(S, D, K, unit[0], xl, xh)) write_row(table, morton, narrow, grid, y, z, xl, xh);
 		}
 	}
 }
@@ -305,6 +306,7 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 		const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
 		const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
 		const bool morton = (J.flags & JOB_MORTON) != 0;
+		const bool narrow = (J.flags & JOB_NARROW) != 0;
 		uint32_t* table = J.table;
 		float tv = lane < 9 ? J.tris[(uint64_t)tri * 9 + lane] : 0.0f;
 		float t[9];
@@ -360,14 +362,14 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 			// share a few lines.
 			const bool has = xh >= xl;
 			const bool wide = has && (morton ? (xh >> 2) - (xl >> 2) >= 4 : (xh >> 5) - (xl >> 5) >= 2);
-			if (has && !wide) write_row(table, morton, grid, y, z, xl, xh);
+			if (has && !wide) write_row(table, morton, narrow, grid, y, z, xl, xh);
 			uint32_t todo = __ballot_sync(FULL, wide);
 			while (todo) {
 				const int src = __ffs(todo) - 1;
 				todo &= todo - 1u;
 				const int ry = __shfl_sync(FULL, y, src), rz = __shfl_sync(FULL, z, src);
 				const int rl = __shfl_sync(FULL, xl, src), rh = __shfl_sync(FULL, xh, src);
-				write_row_warp(table, morton, grid, ry, rz, rl, rh, lane);
+				write_row_warp(table, morton, narrow, grid, ry, rz, rl, rh, lane);
 			}
 		}
 	}

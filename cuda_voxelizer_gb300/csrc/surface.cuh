@@ -340,14 +340,19 @@ __device__ __forceinline__ bool y_interval(const SurfTri& S, float uy, float pz,
 	return true;
 }
 
+// The writers below come in two code types C: uint64_t in general, uint32_t for JOB_NARROW jobs
+// (every index and Morton code below 2^32), which halves the index arithmetic; both give the same
+// words.  The wrappers pick one per job.
+
 // Write the bits of row (y, z), x in [xl, xh].  Linear index x + y*gx + z*gx*gy (:175-178).
-__device__ __forceinline__ void write_row(uint32_t* table, bool morton, const uint32_t* grid, int y, int z, int xl,
-                                          int xh) {
+template <class C>
+__device__ __forceinline__ void write_row_t(uint32_t* table, bool morton, const uint32_t* grid, int y, int z, int xl,
+                                            int xh) {
 	if (morton) {
-		or_span_morton(table, xl, xh, (uint32_t)y, (uint32_t)z);
+		or_span_morton<C>(table, xl, xh, (uint32_t)y, (uint32_t)z);
 	} else {
-		const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
-		or_span(table, base + (uint64_t)xl, base + (uint64_t)xh);
+		const C base = (C)y * grid[0] + (C)z * ((C)grid[1] * grid[0]);
+		or_span<C>(table, base + (C)xl, base + (C)xh);
 	}
 }
 
@@ -355,25 +360,26 @@ __device__ __forceinline__ void write_row(uint32_t* table, bool morton, const ui
 // most two words; the bit of voxel idx is 31 - idx % 32, so a word's bits are the bit-reversed mask
 // shifted by the first voxel's offset.  Morton: one word per 4-voxel x-group (offsets {0, 1, 8, 9}
 // from the group's code, as in or_span_morton).
-__device__ __forceinline__ void write_row_mask(uint32_t* table, bool morton, const uint32_t* grid, int y, int z,
-                                               int x0, uint32_t pm) {
+template <class C>
+__device__ __forceinline__ void write_row_mask_t(uint32_t* table, bool morton, const uint32_t* grid, int y, int z,
+                                                 int x0, uint32_t pm) {
 	if (morton) {
-		const uint64_t yz = (spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2);
+		const C yz = (spread3_t<C>((uint32_t)y) << 1) | (spread3_t<C>((uint32_t)z) << 2);
 		const int x1 = x0 + 31 - __clz(pm);
-		uint64_t xd = spread3((uint32_t)(x0 & ~3));
+		C xd = spread3_t<C>((uint32_t)(x0 & ~3));
 		for (int k = x0 >> 2; k <= (x1 >> 2); k++) {
 			const int sh = (k << 2) - x0;  // mask bit of x = 4k
 			const uint32_t n = (sh >= 0 ? pm >> sh : pm << -sh) & 0xFu;
 			if (n) {
-				const uint64_t code = xd | yz;
+				const C code = xd | yz;
 				const uint32_t m = ((n & 1u) << 31) | ((n & 2u) << 29) | ((n & 4u) << 21) | ((n & 8u) << 19);
 				atomicOr(table + (code >> 5), m >> (uint32_t)(code & 31u));
 			}
-			xd = morton_x_add(xd, kMortonX4);
+			xd = morton_x_add_t<C>(xd, (C)kMortonX4);
 		}
 	} else {
-		const uint64_t idx = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]) + (uint64_t)x0;
-		const uint64_t w = idx >> 5;
+		const C idx = (C)y * grid[0] + (C)z * ((C)grid[1] * grid[0]) + (C)x0;
+		const C w = idx >> 5;
 		const uint32_t off = (uint32_t)(idx & 31u);
 		const uint32_t m0 = __brev(pm) >> off;
 		if (m0) atomicOr(table + w, m0);
@@ -386,27 +392,44 @@ __device__ __forceinline__ void write_row_mask(uint32_t* table, bool morton, con
 
 // write_row by a whole warp (every lane calls it with the same row): lane i takes words
 // w0 + i, w0 + i + 32, ... of the linear span, or x groups k0 + i, ... of the Morton span.
-__device__ __forceinline__ void write_row_warp(uint32_t* table, bool morton, const uint32_t* grid, int y, int z,
-                                               int xl, int xh, uint32_t lane) {
+template <class C>
+__device__ __forceinline__ void write_row_warp_t(uint32_t* table, bool morton, const uint32_t* grid, int y, int z,
+                                                 int xl, int xh, uint32_t lane) {
 	if (morton) {
-		const uint64_t yz = (spread3((uint32_t)y) << 1) | (spread3((uint32_t)z) << 2);
+		const C yz = (spread3_t<C>((uint32_t)y) << 1) | (spread3_t<C>((uint32_t)z) << 2);
 		for (int k = (xl >> 2) + (int)lane; k <= (xh >> 2); k += 32) {
-			const uint64_t code = spread3((uint32_t)(k << 2)) | yz;
+			const C code = spread3_t<C>((uint32_t)(k << 2)) | yz;
 			const int j0 = max(xl - (k << 2), 0), j1 = min(xh - (k << 2), 3);
 			const uint32_t n = (0xFu << j0) & (0xFu >> (3 - j1));
 			const uint32_t m = ((n & 1u) << 31) | ((n & 2u) << 29) | ((n & 4u) << 21) | ((n & 8u) << 19);
 			atomicOr(table + (code >> 5), m >> (uint32_t)(code & 31u));
 		}
 	} else {
-		const uint64_t base = (uint64_t)y * grid[0] + (uint64_t)z * ((uint64_t)grid[1] * grid[0]);
-		const uint64_t lo = base + (uint64_t)xl, hi = base + (uint64_t)xh;
-		const uint64_t w0 = lo >> 5, w1 = hi >> 5;
-		for (uint64_t w = w0 + lane; w <= w1; w += 32) {
+		const C base = (C)y * grid[0] + (C)z * ((C)grid[1] * grid[0]);
+		const C lo = base + (C)xl, hi = base + (C)xh;
+		const C w0 = lo >> 5, w1 = hi >> 5;
+		for (C w = w0 + lane; w <= w1; w += 32) {
 			const uint32_t a = (w == w0) ? (uint32_t)(lo & 31u) : 0u;
 			const uint32_t b = (w == w1) ? (uint32_t)(hi & 31u) : 31u;
 			atomicOr(table + w, span_mask(a, b));
 		}
 	}
+}
+
+__device__ __forceinline__ void write_row(uint32_t* table, bool morton, bool narrow, const uint32_t* grid, int y,
+                                          int z, int xl, int xh) {
+	if (narrow) write_row_t<uint32_t>(table, morton, grid, y, z, xl, xh);
+	else write_row_t<uint64_t>(table, morton, grid, y, z, xl, xh);
+}
+__device__ __forceinline__ void write_row_mask(uint32_t* table, bool morton, bool narrow, const uint32_t* grid, int y,
+                                               int z, int x0, uint32_t pm) {
+	if (narrow) write_row_mask_t<uint32_t>(table, morton, grid, y, z, x0, pm);
+	else write_row_mask_t<uint64_t>(table, morton, grid, y, z, x0, pm);
+}
+__device__ __forceinline__ void write_row_warp(uint32_t* table, bool morton, bool narrow, const uint32_t* grid, int y,
+                                               int z, int xl, int xh, uint32_t lane) {
+	if (narrow) write_row_warp_t<uint32_t>(table, morton, grid, y, z, xl, xh, lane);
+	else write_row_warp_t<uint64_t>(table, morton, grid, y, z, xl, xh, lane);
 }
 
 }  // namespace cvx

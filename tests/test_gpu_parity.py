@@ -174,6 +174,40 @@ def test_non_cubic_grid(ref, solid):
     assert_same(a, b, "non-cubic")
 
 
+def _compare_on_device(ref, t, info, morton):
+    """Engine vs reference kernel on tables too large to copy to the host: compared on the GPU."""
+    d = torch.from_numpy(np.ascontiguousarray(t, dtype=np.float32).reshape(-1)).cuda()
+    a = run_engine(info, d, morton, False)
+    b = run_ref(ref, info, d, morton, False)
+    torch.cuda.synchronize()
+    cv.device_status()
+    differ, set_words = int((a != b).sum()), int(a.count_nonzero())
+    del a, b
+    torch.cuda.empty_cache()
+    return differ, set_words
+
+
+@pytest.mark.parametrize("morton", [False, True])
+def test_grid_2048_indices_above_32_bits(ref, morton):
+    """At 2048^3 Morton codes and linear indices exceed 32 bits: the engine's 64-bit write path
+    (grids up to 2^32 voxels and Morton grids up to 1024 use 32-bit index arithmetic)."""
+    t = np.concatenate([meshgen.soup(7, n=30_000, lmin=0.3 / 2048, lmax=8 / 2048),
+                        meshgen.soup(8, n=200, lmin=8 / 2048, lmax=40 / 2048)]).astype(np.float32)
+    differ, set_words = _compare_on_device(ref, t, info_of(t, 2048), morton)
+    assert differ == 0 and set_words > 0, f"{differ} words differ"
+
+
+def test_linear_grid_of_exactly_2_to_32_voxels(ref):
+    """2048 x 2048 x 1024: the largest linear index is 2^32 - 1, the edge of the 32-bit path."""
+    t = np.concatenate([meshgen.soup(9, n=30_000, lmin=0.3 / 2048, lmax=8 / 2048),
+                        meshgen.soup(10, n=200, lmin=8 / 2048, lmax=40 / 2048)]).astype(np.float32)
+    info = info_of(t, 2048)
+    info.gridsize[2] = 1024
+    info.unit[2] = np.float32((np.float32(info.bbox_max[2]) - np.float32(info.bbox_min[2])) / np.float32(1024))
+    differ, set_words = _compare_on_device(ref, t, info, False)
+    assert differ == 0 and set_words > 0, f"{differ} words differ"
+
+
 @pytest.mark.parametrize("solid", [False, True])
 def test_triangles_outside_bbox(ref, solid):
     """The caller's bbox covers only part of the mesh: surface clamps to the grid; solid columns
