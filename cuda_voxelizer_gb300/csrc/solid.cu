@@ -219,13 +219,16 @@ __device__ __forceinline__ void stage_tile(const LaunchDesc& L, const float* src
 	__syncthreads();
 }
 
-// A small triangle's solid setup parked in shared memory between the classify phases (16 words).
-struct SmallSolid {
+// A small triangle's solid setup parked in shared memory between the classify phases.  15 words
+// padded to 20: records stay 16-byte aligned for vector access, and the 8 lanes of a quarter warp
+// touching 8 records start on banks 0, 20, 8, 28, 16, 4, 24, 12 -- no conflicts (at 16 words, 4-way).
+struct __align__(16) SmallSolid {
 	float nx, ny, nz, v0x, v0y, v0z, ax, ay, bx, by, cx, cy;
 	int y0, z0;
 	uint32_t ext;  // (y1 - y0) | (z1 - z0) << 16
-	uint32_t pad;
+	uint32_t pad[5];
 };
+static_assert(sizeof(SmallSolid) == 80, "SmallSolid stride");
 
 __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
 	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
