@@ -739,8 +739,11 @@ def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
         arr = meshgen.poisson_arrivals(rate, seconds, seed=seed)
         lat = srv.replay(pool, rng.integers(0, len(pool), len(arr)), arr)
         span = float(np.max(arr + lat / 1e3))
+        st = srv.stats()
         return {"rate_per_s": round(rate, 1), "requests": int(len(arr)), "meshes_s": len(arr) / span,
-                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "queue_p99_ms": st["queue_p99_ms"], "generator_late_p99_ms": st["replay_late_p99_ms"],
+                "generator_late_max_ms": st["replay_late_max_ms"]}
 
     def arm(pool, max_batch, max_inflight, fracs, seed0, n_burst):
         mk = lambda: cv.Server(memory_budget_bytes=40 << 30, max_batch=max_batch, max_inflight=max_inflight)
@@ -752,8 +755,10 @@ def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
         res = {"capacity_meshes_s": cap, "max_batch": max_batch, "max_inflight": max_inflight,
                "burst_requests": n_burst, "burst_mean_batch": st["mean_batch"],
                "burst_memory_peak_gib": st["memory_peak"] / 2 ** 30}
-        with mk() as srv:
-            res["sweep"] = [poisson(srv, pool, f * cap, seed0 + i) for i, f in enumerate(fracs)]
+        res["sweep"] = []
+        for i, f in enumerate(fracs):  # a fresh server per rate: its stats cover that rate alone
+            with mk() as srv:
+                res["sweep"].append(poisson(srv, pool, f * cap, seed0 + i))
         return res
 
     rates = copy_rates(torch)

@@ -50,7 +50,9 @@ class CvxServerRequest(ctypes.Structure):
 class CvxServerStats(ctypes.Structure):
     _fields_ = [("completed", u64), ("pending", u64), ("batches", u64), ("mean_batch", ctypes.c_double),
                 ("memory_used", u64), ("memory_budget", u64), ("memory_peak", u64), ("p50_ms", ctypes.c_double),
-                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("meshes_per_s", ctypes.c_double)]
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("meshes_per_s", ctypes.c_double),
+                ("queue_p99_ms", ctypes.c_double), ("replay_late_p99_ms", ctypes.c_double),
+                ("replay_late_max_ms", ctypes.c_double)]
 
 
 class CvxTuning(ctypes.Structure):

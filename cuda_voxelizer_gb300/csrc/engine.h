@@ -37,6 +37,24 @@ struct Prof {
 	void operator()(const char* name, cudaStream_t s) const { mark(ctx, name, s); }
 };
 
+// Launch `kernel` so that it may be scheduled while its predecessor on stream s drains (programmatic
+// stream serialization); the kernel calls pdl_wait() before reading the predecessor's output.
+template <class... KArgs, class... Args>
+inline cudaError_t launch_after(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                                Args... args) {
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(grid);
+	cfg.blockDim = dim3(block);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = s;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Surface launch sequence: classify + cooperative rows.  Counters must be zero.
 cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s, const Prof* prof);
 int surf_rows_blocks_per_sm();

@@ -131,7 +131,7 @@ struct Slot {
 	size_t staging_bytes = 0;
 	bool busy = false;
 	bool finished = false;  // set by the stream callback (under the server mutex)
-	Clock::time_point finish_time;
+	Clock::time_point launch_time, finish_time;
 	std::vector<RequestP> reqs;
 	void* d_rec = nullptr;     // engine records, then the clear list
 	size_t rec_bytes = 0;
@@ -153,6 +153,8 @@ struct cvx_server {
 	std::deque<RequestP> pending;
 	std::unordered_map<uint64_t, RequestP> live;
 	std::vector<double> latencies;
+	std::vector<double> queue_waits;  // submission to the launch of the request's batch (ms)
+	std::vector<double> replay_late;  // cvx_server_replay: submission after the scheduled arrival (ms)
 	uint64_t next_id = 1, completed = 0, batches = 0, batched_requests = 0;
 	Clock::time_point first_arrival, last_done;
 	bool have_first = false, stop = false;
@@ -326,6 +328,7 @@ struct cvx_server {
 			if (r->resident_table) release_work(*r);
 			else unadmit(*r);
 			latencies.push_back(r->latency_ms);
+			queue_waits.push_back(std::chrono::duration<double, std::milli>(sl.launch_time - r->arrival).count());
 			completed++;
 		}
 		last_done = sl.finish_time;
@@ -355,6 +358,7 @@ struct cvx_server {
 				size_t staging_need = 0;
 				if (!fill(sl, &staging_need)) break;  // the head request waits for memory
 				sl.busy = true;
+				sl.launch_time = Clock::now();
 				batches++;
 				batched_requests += sl.reqs.size();
 				lk.unlock();
@@ -530,6 +534,11 @@ cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out) {
 			return CVX_ERR_CUDA;
 		}
 	}
+	// Room for a burst of requests up front: growing these under the server mutex (a rehash of the
+	// request map) would hold up the worker while it is copied.
+	s->live.reserve(1 << 16);
+	s->latencies.reserve(1 << 16);
+	s->queue_waits.reserve(1 << 16);
 	cvx_server* p = s.release();
 	p->worker = std::thread([p] { p->run(); });
 	*out = p;
@@ -582,13 +591,19 @@ cvx_status cvx_server_stats_get(cvx_server* s, cvx_server_stats* out) {
 	out->memory_used = s->arena.used();
 	out->memory_budget = s->arena.size();
 	out->memory_peak = s->arena.peak();
-	if (!s->latencies.empty()) {
-		std::vector<double> v = s->latencies;
+	auto pct = [](std::vector<double> v, double q) {
 		std::sort(v.begin(), v.end());
-		auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * (double)(v.size() - 1) + 0.5))]; };
-		out->p50_ms = pct(0.50);
-		out->p99_ms = pct(0.99);
-		out->max_ms = v.back();
+		return v[std::min(v.size() - 1, (size_t)(q * (double)(v.size() - 1) + 0.5))];
+	};
+	if (!s->queue_waits.empty()) out->queue_p99_ms = pct(s->queue_waits, 0.99);
+	if (!s->replay_late.empty()) {
+		out->replay_late_p99_ms = pct(s->replay_late, 0.99);
+		out->replay_late_max_ms = *std::max_element(s->replay_late.begin(), s->replay_late.end());
+	}
+	if (!s->latencies.empty()) {
+		out->p50_ms = pct(s->latencies, 0.50);
+		out->p99_ms = pct(s->latencies, 0.99);
+		out->max_ms = *std::max_element(s->latencies.begin(), s->latencies.end());
 		const double span = std::chrono::duration<double>(s->last_done - s->first_arrival).count();
 		out->meshes_per_s = span > 0 ? (double)s->completed / span : 0.0;
 	}
@@ -608,19 +623,26 @@ cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint
 		}
 	}
 	std::vector<uint64_t> ids(n);
+	std::vector<double> late(n);
 	const Clock::time_point t0 = Clock::now();
 	cvx_status first_err = CVX_OK;
 	std::string first_msg;
 	for (uint32_t i = 0; i < n; i++) {
 		const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
 		if (due - Clock::now() > std::chrono::microseconds(300)) std::this_thread::sleep_until(due - std::chrono::microseconds(200));
-		while (Clock::now() < due) {
+		Clock::time_point now;
+		while ((now = Clock::now()) < due) {
 		}
+		late[i] = std::chrono::duration<double, std::milli>(now - due).count();
 		const cvx_status st = s->submit(&reqs[i], due, &ids[i], reqs[i].h_table == nullptr);
 		if (st != CVX_OK) {
 			for (uint32_t k = 0; k < i; k++) s->wait(ids[k], -1.0, nullptr);
 			return st;
 		}
+	}
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		s->replay_late.insert(s->replay_late.end(), late.begin(), late.end());
 	}
 	for (uint32_t i = 0; i < n; i++) {
 		const cvx_status st = s->wait(ids[i], -1.0, &latency_ms[i]);

@@ -110,6 +110,7 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 	__shared__ uint32_t s_warp[kTile / 32];
 	__shared__ uint32_t s_fit;  // end of the item list: the first local triangle that did not fit
 	__shared__ __align__(8) uint64_t s_bar;
+	pdl_trigger();  // surf_rows may be scheduled as this grid's last wave runs
 	const uint32_t tile = blockIdx.x;
 	const uint32_t j = job_of_tile(L, tile);
 	const JobDesc& J = job_at(L, j);
@@ -253,6 +254,7 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 
 template <class P>
 __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant__ LaunchDesc L) {
+	pdl_wait();  // the queue is surf_classify's output
 	const uint32_t lane = threadIdx.x & 31u;
 	Counters* C = L.scr.ctr;
 	// One thread per CTA reads the queue counters (thousands of warps reading one line would
@@ -388,7 +390,8 @@ static cudaError_t launch_surface_t(const LaunchDesc& L, const Tune& tune, int r
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("surf_classify", s);
-	surf_rows<P><<<rows_grid, kRowsThreads, 0, s>>>(L);
+	e = launch_after(surf_rows<P>, (unsigned)rows_grid, kRowsThreads, 0, s, L);
+	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("surf_rows", s);
 	return cudaGetLastError();
 }

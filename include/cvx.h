@@ -189,6 +189,9 @@ typedef struct cvx_server_stats {
 	uint64_t memory_peak;                 /* most arena bytes ever in use at once */
 	double p50_ms, p99_ms, max_ms;        /* latency, submission to table written */
 	double meshes_per_s;                  /* completed / (last completion - first submission) */
+	double queue_p99_ms;                  /* submission to the launch of the request's batch, p99 */
+	double replay_late_p99_ms;            /* cvx_server_replay: how late its submissions were against */
+	double replay_late_max_ms;            /*   the schedule (p99, maximum); latency counts from the schedule */
 } cvx_server_stats;
 /* CVX_ERR_OUT_OF_MEMORY if the budget cannot be allocated. */
 cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out);

@@ -105,6 +105,9 @@ def test_server_open_loop_replay():
         st = srv.stats()
     assert len(lat) == len(arrivals) > 20 and np.all(lat > 0) and np.all(np.isfinite(lat))
     assert st["completed"] == len(arrivals)
+    # the queue wait is part of the latency; the generator's own lateness is reported beside it
+    assert 0 <= st["queue_p99_ms"] <= st["max_ms"]
+    assert 0 <= st["replay_late_p99_ms"] <= st["replay_late_max_ms"]
     for s, (info, t, tab) in zip(specs, host):
         if np.any(index == specs.index(s)):
             assert torch.equal(tab, _alone(info, t, s.morton, s.solid)), s
