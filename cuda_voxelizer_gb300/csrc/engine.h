@@ -14,6 +14,7 @@ constexpr uint32_t kRowsThreads = 256; // threads per cooperative CTA
 constexpr uint32_t kColsPerItem = 256; // solid columns per work item
 constexpr uint32_t kSmallRows = 16;    // surface: rows of a small triangle (every voxel tested)
 constexpr uint32_t kLocalRows = 64;    // surface: rows of a local triangle (row intervals), classify kernel
+constexpr uint32_t kMaskRowVoxels = 16; // surface: local rows up to this long test every voxel (the pass mask holds 16)
 constexpr uint32_t kSmallCols = 16;    // solid: columns of a triangle handled in the classify kernel
 
 // Device-side check codes written to Counters::error.

@@ -238,7 +238,9 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 		if (yz_fail_bits<P>(S, py, pz)) continue;
 		RowK K;
 		row_consts<P>(S, py, pz, K);
-		if (small) {
+		// Rows of at most kMaskRowVoxels voxels test every voxel (a local triangle's short rows too):
+		// cheaper than setting up the crossing estimates of an exact interval search.
+		if (small || S.bx1 - S.bx0 < (int)kMaskRowVoxels) {
 			// src/voxelize.cu:136-183: every voxel of the row (at most 16), as a pass mask
 			uint32_t pm = 0;
 			for (int i = 0; i <= S.bx1 - S.bx0; i++) pm |= (uint32_t)voxel_pass<P>(S, K, unit[0], S.bx0 + i) << i;
