@@ -742,7 +742,8 @@ def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
         st = srv.stats()
         return {"rate_per_s": round(rate, 1), "requests": int(len(arr)), "meshes_s": len(arr) / span,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "queue_p99_ms": st["queue_p99_ms"], "generator_late_p99_ms": st["replay_late_p99_ms"],
+                "queue_p99_ms": st["queue_p99_ms"], "batch_service_p50_ms": st["service_p50_ms"],
+                "batch_service_p99_ms": st["service_p99_ms"], "generator_late_p99_ms": st["replay_late_p99_ms"],
                 "generator_late_max_ms": st["replay_late_max_ms"]}
 
     def arm(pool, max_batch, max_inflight, fracs, seed0, n_burst):
@@ -770,6 +771,9 @@ def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
            "copy_rates": rates, "bytes_per_request": {"in": per_req_in, "out": per_req_out}}
     fr = (0.25, 0.5, 0.75, 0.9)
     host = {"served": arm(host_pool, 4, 32, fr, 0, 4096), "plain": arm(host_pool, 1, 1, (0.5, 0.9), 10, 512)}
+    # the link's rates again after the host-buffer arms: the machine's host memory is shared, and a
+    # drop here shows up as longer batch service times and queueing in the sweep above
+    out["copy_rates_after_host_arms"] = copy_rates(torch)
     host["roofline_meshes_s"] = min(copy_cap, plan_meshes_s)
     host["served_frac_of_roofline"] = host["served"]["capacity_meshes_s"] / host["roofline_meshes_s"]
     host["served_vs_plain_capacity"] = host["served"]["capacity_meshes_s"] / host["plain"]["capacity_meshes_s"]

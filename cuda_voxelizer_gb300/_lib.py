@@ -52,7 +52,8 @@ class CvxServerStats(ctypes.Structure):
                 ("memory_used", u64), ("memory_budget", u64), ("memory_peak", u64), ("p50_ms", ctypes.c_double),
                 ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("meshes_per_s", ctypes.c_double),
                 ("queue_p99_ms", ctypes.c_double), ("replay_late_p99_ms", ctypes.c_double),
-                ("replay_late_max_ms", ctypes.c_double)]
+                ("replay_late_max_ms", ctypes.c_double), ("service_p50_ms", ctypes.c_double),
+                ("service_p99_ms", ctypes.c_double)]
 
 
 class CvxTuning(ctypes.Structure):

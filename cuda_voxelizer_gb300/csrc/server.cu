@@ -154,6 +154,7 @@ struct cvx_server {
 	std::unordered_map<uint64_t, RequestP> live;
 	std::vector<double> latencies;
 	std::vector<double> queue_waits;  // submission to the launch of the request's batch (ms)
+	std::vector<double> services;     // launch to completion of each batch (ms)
 	std::vector<double> replay_late;  // cvx_server_replay: submission after the scheduled arrival (ms)
 	uint64_t next_id = 1, completed = 0, batches = 0, batched_requests = 0;
 	Clock::time_point first_arrival, last_done;
@@ -332,6 +333,7 @@ struct cvx_server {
 			completed++;
 		}
 		last_done = sl.finish_time;
+		services.push_back(std::chrono::duration<double, std::milli>(sl.finish_time - sl.launch_time).count());
 		arena.release(sl.d_rec);
 		sl.d_rec = nullptr;
 		sl.d_clears = nullptr;
@@ -539,6 +541,7 @@ cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out) {
 	s->live.reserve(1 << 16);
 	s->latencies.reserve(1 << 16);
 	s->queue_waits.reserve(1 << 16);
+	s->services.reserve(1 << 16);
 	cvx_server* p = s.release();
 	p->worker = std::thread([p] { p->run(); });
 	*out = p;
@@ -596,6 +599,10 @@ cvx_status cvx_server_stats_get(cvx_server* s, cvx_server_stats* out) {
 		return v[std::min(v.size() - 1, (size_t)(q * (double)(v.size() - 1) + 0.5))];
 	};
 	if (!s->queue_waits.empty()) out->queue_p99_ms = pct(s->queue_waits, 0.99);
+	if (!s->services.empty()) {
+		out->service_p50_ms = pct(s->services, 0.50);
+		out->service_p99_ms = pct(s->services, 0.99);
+	}
 	if (!s->replay_late.empty()) {
 		out->replay_late_p99_ms = pct(s->replay_late, 0.99);
 		out->replay_late_max_ms = *std::max_element(s->replay_late.begin(), s->replay_late.end());
