@@ -476,10 +476,13 @@ cvx_status cvx::batch_scratch_bytes(const cvx_job* jobs, uint32_t n_jobs, size_t
 }
 
 cvx_status cvx::run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* const* flips, void* d_rec,
-                             size_t rec_bytes, void* h_staging, size_t staging_bytes, cudaStream_t s) {
+                             size_t rec_bytes, void* h_staging, size_t staging_bytes, cudaStream_t s,
+                             bool tables_zeroed) {
 	std::vector<JobDesc> surf, solid;
 	cvx_status st = collect_jobs(jobs, n_jobs, flips, surf, solid);
 	if (st != CVX_OK) return st;
+	if (tables_zeroed)
+		for (JobDesc& j : solid) j.flags |= JOB_TABLE_ZERO;
 	if (surf.empty() && solid.empty()) return CVX_OK;
 	if (!solid.empty() && !flips) return fail(CVX_ERR_INVALID_VALUE, "solid jobs need flip tables");
 	const uint64_t cap = queue_cap(surf, solid);
@@ -737,6 +740,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		tables.push_back({jobs[i].d_table, words_of(jobs[i].info)});
 		if (jobs[i].info.n_triangles == 0) continue;
 		JobDesc j = make_job(jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
+		if (flags & CVX_PLAN_CLEAR_TABLES) j.flags |= JOB_TABLE_ZERO;  // the graph zeroes it first
 		(jobs[i].solid ? solid : surf).push_back(j);
 	}
 	DevState dev;
@@ -1032,6 +1036,7 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 		v.n_triangles = b1 - b0;
 		JobDesc j = make_job(v, jobs[i].d_triangles + 9 * b0, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
 		j.flips = flips[i];
+		j.flags |= JOB_TABLE_ZERO;  // the plan zeroes every table first
 		return j;
 	};
 	// The compute stream's steps.  Jobs without triangles are complete once cleared.

@@ -63,7 +63,10 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 // JOB_NARROW: every voxel index of the job fits 32 bits (linear: gx*gy*gz <= 2^32; Morton: a cubic
 // grid of at most 1024), so the surface writes compute indices and Morton codes in 32-bit
 // arithmetic.  Set by the host; a hint only (the 64-bit path gives the same words).
-enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u };
+// JOB_TABLE_ZERO: the engine zeroed the job's table earlier in the same launch sequence (plans that
+// clear their tables, host plans, server batches), so the solid passes store their words instead of
+// XOR-ing them into the table (same result, no read) and skip words that resolve to zero.
+enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u, JOB_TABLE_ZERO = 8u };
 
 // One mesh voxelization.  Plain data, uploaded as an array for batches or passed by value for a
 // single mesh.
@@ -76,7 +79,7 @@ struct JobDesc {
 	float unit[3];
 	float inv_unit[3];     // 1.0f / unit, correctly rounded (host); only used for the exactly checked div_trunc
 	uint32_t grid[3];
-	uint32_t flags;        // JOB_MORTON | JOB_SOLID | JOB_NARROW
+	uint32_t flags;        // JOB_MORTON | JOB_SOLID | JOB_NARROW | JOB_TABLE_ZERO
 	uint32_t tile_begin;   // first triangle tile of this job in the launch's tile space
 	uint32_t unit_begin;   // solid: first resolve unit of this job in the launch's unit space
 	uint64_t mword_begin;  // solid Morton, g < 32: first Morton word in the launch's word space

@@ -300,7 +300,7 @@ struct cvx_server {
 		if (ok) ok = cuda_ok(cvx::launch_clear(sl.d_clears, n_ranges, chunks, st), "clear tables");
 		if (ok) {
 			const cvx_status rs = cvx::run_batch_on(jobs.data(), (uint32_t)jobs.size(), flips.data(), sl.d_rec,
-			                                        sl.rec_bytes, sl.staging, sl.staging_bytes, st);
+			                                        sl.rec_bytes, sl.staging, sl.staging_bytes, st, true);
 			if (rs != CVX_OK) {
 				fail_batch(sl, rs, cvx_last_error_message());
 				ok = false;

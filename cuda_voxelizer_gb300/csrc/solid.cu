@@ -469,12 +469,20 @@ __device__ __forceinline__ uint32_t resolve_word(uint32_t t, uint32_t& carry) {
 
 // Linear jobs: table ^= resolved, toggles cleared.  Morton jobs: toggles replaced by the resolved
 // bits for solid_morton_* to gather.
+// XOR a resolved word into the table (the reference's semantics: the caller's table is XORed), or
+// store it when the engine zeroed the table itself (JOB_TABLE_ZERO): same words, no read.
+__device__ __forceinline__ void xor_out(uint32_t* dest, uint64_t w, uint32_t v, bool zero) {
+	if (!v) return;
+	if (zero) dest[w] = v;
+	else dest[w] ^= v;
+}
+
 __device__ __forceinline__ void resolve_store(uint32_t* flips, uint32_t* dest, uint64_t w, uint32_t t, uint32_t res,
-                                              bool morton) {
+                                              bool morton, bool zero) {
 	if (morton) {
 		if (res != t) flips[w] = res;
 	} else {
-		if (res) dest[w] ^= res;
+		xor_out(dest, w, res, zero);
 		if (t) flips[w] = 0u;
 	}
 }
@@ -492,6 +500,7 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 	const uint64_t gx = J.grid[0];
 	const uint64_t rows = (uint64_t)J.grid[1] * J.grid[2];
 	const bool morton = (J.flags & JOB_MORTON) != 0;
+	const bool zero = (J.flags & JOB_TABLE_ZERO) != 0;
 	uint32_t* flips = J.flips;
 	uint32_t* dest = J.table;
 	const uint64_t u = unit_id - J.unit_begin;
@@ -509,6 +518,9 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 				const uint32_t r2 = resolve_word(t.z, carry), r3 = resolve_word(t.w, carry);
 				if (morton) {
 					*reinterpret_cast<uint4*>(flips + w0 + i) = make_uint4(r0, r1, r2, r3);
+				} else if (zero) {
+					if (r0 | r1 | r2 | r3) *reinterpret_cast<uint4*>(dest + w0 + i) = make_uint4(r0, r1, r2, r3);
+					if (t.x | t.y | t.z | t.w) *reinterpret_cast<uint4*>(flips + w0 + i) = make_uint4(0u, 0u, 0u, 0u);
 				} else {
 					uint4 d = *reinterpret_cast<const uint4*>(dest + w0 + i);
 					d.x ^= r0; d.y ^= r1; d.z ^= r2; d.w ^= r3;
@@ -520,7 +532,7 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 			for (uint32_t i = 0; i < wpr; i++) {
 				const uint32_t t = flips[w0 + i];
 				if (t == 0u && carry == 0u) continue;
-				resolve_store(flips, dest, w0 + i, t, resolve_word(t, carry), morton);
+				resolve_store(flips, dest, w0 + i, t, resolve_word(t, carry), morton, zero);
 			}
 		}
 	} else {
@@ -545,7 +557,7 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 				carry ^= (t >> (31 - k)) & 1u;
 				res |= carry << (31 - k);
 			}
-			resolve_store(flips, dest, w, t, res, morton);
+			resolve_store(flips, dest, w, t, res, morton, zero);
 		}
 	}
 }
@@ -608,7 +620,7 @@ __global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant_
 					const uint32_t nib = (row >> (28u - 4u * X)) & 0xFu;
 					out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 				}
-			if (out) dest[m] ^= out;
+			xor_out(dest, m, out, (J.flags & JOB_TABLE_ZERO) != 0);
 		}
 	}
 }
@@ -674,7 +686,7 @@ __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__
 				const uint32_t nib = (rw >> (28u - xoff)) & 0xFu;
 				out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 			}
-		if (out) J.table[(blk << 7) + m] ^= out;
+		xor_out(J.table, (blk << 7) + m, out, (J.flags & JOB_TABLE_ZERO) != 0);
 	}
 }
 
@@ -698,7 +710,7 @@ __global__ void __launch_bounds__(256) solid_morton_small(const __grid_constant_
 		const uint64_t lin = x + g * (y + g * z);
 		out |= ((flips[lin >> 5] >> (31u - (uint32_t)(lin & 31u))) & 1u) << (31u - i);
 	}
-	if (out) J.table[m] ^= out;
+	xor_out(J.table, m, out, (J.flags & JOB_TABLE_ZERO) != 0);
 }
 
 // Morton jobs with g < 32: clear the resolved flip table, one thread per resolve unit (the larger

@@ -319,6 +319,28 @@ def test_plan_equals_single_calls_and_replays():
     plan.close()
 
 
+def test_plan_without_clearing_keeps_xor_semantics():
+    """A plan that does not clear its tables ORs (surface) and XORs (solid) into them like plain
+    calls: launched twice, surface tables are unchanged and solid tables return to zero."""
+    jobs = _mixed_jobs()
+    for j in jobs:
+        j.table.zero_()
+    plan = cv.Plan(jobs, clear_tables=False)
+    plan.launch()
+    torch.cuda.synchronize()
+    once = [j.table.clone() for j in jobs]
+    for j, t in zip(jobs, once):
+        assert torch.equal(t, run_engine(j.info, j.triangles, j.morton, j.solid))
+    plan.launch()
+    torch.cuda.synchronize()
+    for j, t in zip(jobs, once):
+        if j.solid:
+            assert int(j.table.count_nonzero()) == 0
+        else:
+            assert torch.equal(j.table, t)
+    plan.close()
+
+
 @pytest.mark.parametrize("solid", [False, True])
 def test_caller_workspace_equals_internal(solid):
     t = meshgen.soup(20, n=20000, lmin=0.002, lmax=0.3)
