@@ -32,6 +32,8 @@ constexpr double kFloatError = 0.000001;  // src/voxelize_solid.cu:13 (a double 
 // For a float f, (double)f < 0.000001 exactly when f <= 0x1.0c6f7ap-20f, the largest float below the
 // double 1e-6 (floats are exact in double, and 0x1.0c6f7ap-20 < 1e-6 < its successor).
 constexpr float kFloatErrorBelow = 0x1.0c6f7ap-20f;
+static_assert((double)kFloatErrorBelow < kFloatError && (double)0x1.0c6f7cp-20f >= kFloatError,
+              "kFloatErrorBelow is the largest float below the reference's float_error");
 
 // floor((double)q - 0.5) and ceil(...) for a float q: q - 0.5f is exact in float when |q| < 2^22
 // (its ulp is at most 0.5 there), so float floor/ceil give the double result; else use double.
