@@ -733,7 +733,8 @@ def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
         return {"rate_per_s": round(rate, 1), "requests": int(len(arr)), "meshes_s": len(arr) / span,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                 "queue_p99_ms": st["queue_p99_ms"], "batch_service_p50_ms": st["service_p50_ms"],
-                "batch_service_p99_ms": st["service_p99_ms"], "generator_late_p99_ms": st["replay_late_p99_ms"],
+                "batch_service_p99_ms": st["service_p99_ms"], "batch_issue_p50_us": st["issue_p50_us"],
+                "mean_batch": st["mean_batch"], "generator_late_p99_ms": st["replay_late_p99_ms"],
                 "generator_late_max_ms": st["replay_late_max_ms"]}
 
     def arm(pool, max_batch, max_inflight, fracs, seed0, n_burst):
@@ -744,7 +745,7 @@ def bench_serve(cv, meshgen, torch, mix, seconds, plan_meshes_s):
             cap = burst(srv, pool, n_burst)
             st = srv.stats()
         res = {"capacity_meshes_s": cap, "max_batch": max_batch, "max_inflight": max_inflight,
-               "burst_requests": n_burst, "burst_mean_batch": st["mean_batch"],
+               "burst_requests": n_burst, "burst_mean_batch": st["mean_batch"], "burst_issue_p50_us": st["issue_p50_us"],
                "burst_memory_peak_gib": st["memory_peak"] / 2 ** 30}
         res["sweep"] = []
         for i, f in enumerate(fracs):  # a fresh server per rate: its stats cover that rate alone

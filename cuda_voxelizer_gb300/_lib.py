@@ -53,7 +53,7 @@ class CvxServerStats(ctypes.Structure):
                 ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("meshes_per_s", ctypes.c_double),
                 ("queue_p99_ms", ctypes.c_double), ("replay_late_p99_ms", ctypes.c_double),
                 ("replay_late_max_ms", ctypes.c_double), ("service_p50_ms", ctypes.c_double),
-                ("service_p99_ms", ctypes.c_double)]
+                ("service_p99_ms", ctypes.c_double), ("issue_p50_us", ctypes.c_double)]
 
 
 class CvxTuning(ctypes.Structure):

@@ -155,6 +155,7 @@ struct cvx_server {
 	std::vector<double> latencies;
 	std::vector<double> queue_waits;  // submission to the launch of the request's batch (ms)
 	std::vector<double> services;     // launch to completion of each batch (ms)
+	std::vector<double> issue_us;     // worker time spent issuing each batch's work (us)
 	std::vector<double> replay_late;  // cvx_server_replay: submission after the scheduled arrival (ms)
 	uint64_t next_id = 1, completed = 0, batches = 0, batched_requests = 0;
 	Clock::time_point first_arrival, last_done;
@@ -364,8 +365,11 @@ struct cvx_server {
 				batches++;
 				batched_requests += sl.reqs.size();
 				lk.unlock();
+				const Clock::time_point t_issue = Clock::now();
 				launch(sl, staging_need);
+				const double us = std::chrono::duration<double, std::micro>(Clock::now() - t_issue).count();
 				lk.lock();
+				issue_us.push_back(us);
 				launched = true;
 			}
 			if (stop && pending.empty() && !any_busy()) break;
@@ -542,6 +546,7 @@ cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out) {
 	s->latencies.reserve(1 << 16);
 	s->queue_waits.reserve(1 << 16);
 	s->services.reserve(1 << 16);
+	s->issue_us.reserve(1 << 16);
 	cvx_server* p = s.release();
 	p->worker = std::thread([p] { p->run(); });
 	*out = p;
@@ -603,6 +608,7 @@ cvx_status cvx_server_stats_get(cvx_server* s, cvx_server_stats* out) {
 		out->service_p50_ms = pct(s->services, 0.50);
 		out->service_p99_ms = pct(s->services, 0.99);
 	}
+	if (!s->issue_us.empty()) out->issue_p50_us = pct(s->issue_us, 0.50);
 	if (!s->replay_late.empty()) {
 		out->replay_late_p99_ms = pct(s->replay_late, 0.99);
 		out->replay_late_max_ms = *std::max_element(s->replay_late.begin(), s->replay_late.end());

@@ -193,6 +193,7 @@ typedef struct cvx_server_stats {
 	double replay_late_p99_ms;            /* cvx_server_replay: how late its submissions were against */
 	double replay_late_max_ms;            /*   the schedule (p99, maximum); latency counts from the schedule */
 	double service_p50_ms, service_p99_ms; /* a batch's launch to completion (copies in, kernels, copies out) */
+	double issue_p50_us;                  /* host time the worker spends issuing one batch's work */
 } cvx_server_stats;
 /* CVX_ERR_OUT_OF_MEMORY if the budget cannot be allocated. */
 cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out);

@@ -109,6 +109,7 @@ def test_server_open_loop_replay():
     assert 0 <= st["queue_p99_ms"] <= st["max_ms"]
     assert 0 <= st["replay_late_p99_ms"] <= st["replay_late_max_ms"]
     assert 0 < st["service_p50_ms"] <= st["service_p99_ms"] <= st["max_ms"]
+    assert st["issue_p50_us"] > 0
     for s, (info, t, tab) in zip(specs, host):
         if np.any(index == specs.index(s)):
             assert torch.equal(tab, _alone(info, t, s.morton, s.solid)), s
