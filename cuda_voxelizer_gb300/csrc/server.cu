@@ -495,6 +495,9 @@ struct cvx_server {
 	}
 };
 
+static_assert(sizeof(cvx_server_stats) == 136, "cvx_server_stats layout (the Python binding mirrors it)");
+static_assert(sizeof(cvx_server_request) == 96, "cvx_server_request layout (the Python binding mirrors it)");
+
 extern "C" {
 
 cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out) {

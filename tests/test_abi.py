@@ -146,3 +146,9 @@ def test_host_plan_validation_answers_without_a_gpu():
     job.morton = 1
     job.info.gridsize[1] = 32  # Morton order needs a cubic power-of-two grid
     assert _lib.lib.cvx_plan_create_host(ctypes.byref(job), 1, 0, ctypes.byref(h)) != 0
+
+
+def test_server_stats_struct_layout():
+    S = _lib.CvxServerStats
+    assert ctypes.sizeof(S) == 136  # static_assert in the library
+    assert S.meshes_per_s.offset == 80 and S.queue_p99_ms.offset == 88 and S.issue_p50_us.offset == 128
