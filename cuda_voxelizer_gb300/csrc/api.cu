@@ -248,7 +248,8 @@ void finish_group(Group& g, bool solid) {
 		g.tris += j.n_tri;
 		if (solid) {
 			j.unit_begin = unit;
-			unit += (uint32_t)solid_units(j.grid).units;
+			// Morton slab grids are resolved by solid_morton_slab alone: no resolve units
+			if (!((j.flags & JOB_MORTON) && morton_slab_grid(j.grid[0]))) unit += (uint32_t)solid_units(j.grid).units;
 			j.mword_begin = mw;
 			j.mbrick_begin = mb;
 			j.mslab_begin = ms;

@@ -169,6 +169,7 @@ extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const 
 	L.n_units = (uint32_t)su.units;
 	if (morton) {
 		if (morton_slab_grid(g0)) {
+			L.n_units = 0;  // solid_morton_slab resolves these grids alone
 			L.n_mslabs = (g0 / 16) * (g0 / 16);
 			L.slab_smem = (256u * ((uint32_t)(g0 / 32) | 1u) + kSlabSkewWords) * 4u;
 		} else if (g0 >= 32) {
