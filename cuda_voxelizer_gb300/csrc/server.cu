@@ -125,6 +125,24 @@ struct Request {
 };
 using RequestP = std::shared_ptr<Request>;
 
+// The most recent kWindow samples of a statistic (a ring once full): a long-running server keeps
+// bounded memory, and its percentiles describe recent traffic.
+struct Window {
+	static constexpr size_t kWindow = size_t(1) << 20;
+	std::vector<double> v;
+	size_t next = 0;
+	Window() { v.reserve(size_t(1) << 16); }
+	void push(double x) {
+		if (v.size() < kWindow) {
+			v.push_back(x);
+		} else {
+			v[next] = x;
+			next = (next + 1) % kWindow;
+		}
+	}
+	bool empty() const { return v.empty(); }
+};
+
 struct Slot {
 	cudaStream_t stream = nullptr;
 	void* staging = nullptr;  // pinned job staging for the engine
@@ -152,11 +170,11 @@ struct cvx_server {
 	std::condition_variable cv_work, cv_done;
 	std::deque<RequestP> pending;
 	std::unordered_map<uint64_t, RequestP> live;
-	std::vector<double> latencies;
-	std::vector<double> queue_waits;  // submission to the launch of the request's batch (ms)
-	std::vector<double> services;     // launch to completion of each batch (ms)
-	std::vector<double> issue_us;     // worker time spent issuing each batch's work (us)
-	std::vector<double> replay_late;  // cvx_server_replay: submission after the scheduled arrival (ms)
+	Window latencies;
+	Window queue_waits;  // submission to the launch of the request's batch (ms)
+	Window services;     // launch to completion of each batch (ms)
+	Window issue_us;     // worker time spent issuing each batch's work (us)
+	Window replay_late;  // cvx_server_replay: submission after the scheduled arrival (ms)
 	uint64_t next_id = 1, completed = 0, batches = 0, batched_requests = 0;
 	Clock::time_point first_arrival, last_done;
 	bool have_first = false, stop = false;
@@ -329,12 +347,12 @@ struct cvx_server {
 			r->done = true;
 			if (r->resident_table) release_work(*r);
 			else unadmit(*r);
-			latencies.push_back(r->latency_ms);
-			queue_waits.push_back(std::chrono::duration<double, std::milli>(sl.launch_time - r->arrival).count());
+			latencies.push(r->latency_ms);
+			queue_waits.push(std::chrono::duration<double, std::milli>(sl.launch_time - r->arrival).count());
 			completed++;
 		}
 		last_done = sl.finish_time;
-		services.push_back(std::chrono::duration<double, std::milli>(sl.finish_time - sl.launch_time).count());
+		services.push(std::chrono::duration<double, std::milli>(sl.finish_time - sl.launch_time).count());
 		arena.release(sl.d_rec);
 		sl.d_rec = nullptr;
 		sl.d_clears = nullptr;
@@ -369,7 +387,7 @@ struct cvx_server {
 				launch(sl, staging_need);
 				const double us = std::chrono::duration<double, std::micro>(Clock::now() - t_issue).count();
 				lk.lock();
-				issue_us.push_back(us);
+				issue_us.push(us);
 				launched = true;
 			}
 			if (stop && pending.empty() && !any_busy()) break;
@@ -546,10 +564,6 @@ cvx_status cvx_server_create(const cvx_server_config* cfg, cvx_server** out) {
 	// Room for a burst of requests up front: growing these under the server mutex (a rehash of the
 	// request map) would hold up the worker while it is copied.
 	s->live.reserve(1 << 16);
-	s->latencies.reserve(1 << 16);
-	s->queue_waits.reserve(1 << 16);
-	s->services.reserve(1 << 16);
-	s->issue_us.reserve(1 << 16);
 	cvx_server* p = s.release();
 	p->worker = std::thread([p] { p->run(); });
 	*out = p;
@@ -593,35 +607,45 @@ cvx_status cvx_server_stats_get(cvx_server* s, cvx_server_stats* out) {
 		cvx::set_message("cvx_server_stats_get: null argument");
 		return CVX_ERR_INVALID_VALUE;
 	}
-	std::lock_guard<std::mutex> lk(s->mu);
 	std::memset(out, 0, sizeof(*out));
-	out->completed = s->completed;
-	out->pending = s->pending.size();
-	out->batches = s->batches;
-	out->mean_batch = s->batches ? (double)s->batched_requests / (double)s->batches : 0.0;
-	out->memory_used = s->arena.used();
-	out->memory_budget = s->arena.size();
-	out->memory_peak = s->arena.peak();
-	auto pct = [](std::vector<double> v, double q) {
-		std::sort(v.begin(), v.end());
+	// Copy under the lock, sort outside it: the worker and the completion callbacks need the mutex.
+	std::vector<double> lat, queue, svc, issue, late;
+	double span = 0.0;
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		out->completed = s->completed;
+		out->pending = s->pending.size();
+		out->batches = s->batches;
+		out->mean_batch = s->batches ? (double)s->batched_requests / (double)s->batches : 0.0;
+		out->memory_used = s->arena.used();
+		out->memory_budget = s->arena.size();
+		out->memory_peak = s->arena.peak();
+		lat = s->latencies.v;
+		queue = s->queue_waits.v;
+		svc = s->services.v;
+		issue = s->issue_us.v;
+		late = s->replay_late.v;
+		if (!lat.empty()) span = std::chrono::duration<double>(s->last_done - s->first_arrival).count();
+	}
+	auto pct = [](std::vector<double>& v, double q) {
 		return v[std::min(v.size() - 1, (size_t)(q * (double)(v.size() - 1) + 0.5))];
 	};
-	if (!s->queue_waits.empty()) out->queue_p99_ms = pct(s->queue_waits, 0.99);
-	if (!s->services.empty()) {
-		out->service_p50_ms = pct(s->services, 0.50);
-		out->service_p99_ms = pct(s->services, 0.99);
+	for (std::vector<double>* v : {&lat, &queue, &svc, &issue, &late}) std::sort(v->begin(), v->end());
+	if (!queue.empty()) out->queue_p99_ms = pct(queue, 0.99);
+	if (!svc.empty()) {
+		out->service_p50_ms = pct(svc, 0.50);
+		out->service_p99_ms = pct(svc, 0.99);
 	}
-	if (!s->issue_us.empty()) out->issue_p50_us = pct(s->issue_us, 0.50);
-	if (!s->replay_late.empty()) {
-		out->replay_late_p99_ms = pct(s->replay_late, 0.99);
-		out->replay_late_max_ms = *std::max_element(s->replay_late.begin(), s->replay_late.end());
+	if (!issue.empty()) out->issue_p50_us = pct(issue, 0.50);
+	if (!late.empty()) {
+		out->replay_late_p99_ms = pct(late, 0.99);
+		out->replay_late_max_ms = late.back();
 	}
-	if (!s->latencies.empty()) {
-		out->p50_ms = pct(s->latencies, 0.50);
-		out->p99_ms = pct(s->latencies, 0.99);
-		out->max_ms = *std::max_element(s->latencies.begin(), s->latencies.end());
-		const double span = std::chrono::duration<double>(s->last_done - s->first_arrival).count();
-		out->meshes_per_s = span > 0 ? (double)s->completed / span : 0.0;
+	if (!lat.empty()) {
+		out->p50_ms = pct(lat, 0.50);
+		out->p99_ms = pct(lat, 0.99);
+		out->max_ms = lat.back();
+		out->meshes_per_s = span > 0 ? (double)out->completed / span : 0.0;
 	}
 	return CVX_OK;
 }
@@ -658,7 +682,7 @@ cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint
 	}
 	{
 		std::lock_guard<std::mutex> lk(s->mu);
-		s->replay_late.insert(s->replay_late.end(), late.begin(), late.end());
+		for (double x : late) s->replay_late.push(x);
 	}
 	for (uint32_t i = 0; i < n; i++) {
 		const cvx_status st = s->wait(ids[i], -1.0, &latency_ms[i]);

@@ -187,7 +187,8 @@ typedef struct cvx_server_stats {
 	double mean_batch;                    /* requests per batch */
 	uint64_t memory_used, memory_budget;  /* arena bytes now in use / in total */
 	uint64_t memory_peak;                 /* most arena bytes ever in use at once */
-	double p50_ms, p99_ms, max_ms;        /* latency, submission to table written */
+	double p50_ms, p99_ms, max_ms;        /* latency, submission to table written; these and the
+	                                       * other percentiles cover the last 2^20 samples */
 	double meshes_per_s;                  /* completed / (last completion - first submission) */
 	double queue_p99_ms;                  /* submission to the launch of the request's batch, p99 */
 	double replay_late_p99_ms;            /* cvx_server_replay: how late its submissions were against */
