@@ -77,6 +77,7 @@ SIGNATURES = {
     "cvx_voxelize_ws": (c_status, [ctypes.POINTER(CvxVoxinfo), vp, vp, ctypes.c_int, ctypes.c_int, vp, u64, vp]),
     "cvx_voxelize_solid_noalloc": (c_status, [ctypes.POINTER(CvxVoxinfo), vp, vp, ctypes.c_int, vp]),
     "cvx_device_status": (c_status, [vp]),
+    "cvx_stream_release": (c_status, [vp]),
     "cvx_voxelize_batch": (c_status, [ctypes.POINTER(CvxJob), u32, vp]),
     "cvx_plan_create": (c_status, [ctypes.POINTER(CvxJob), u32, u32, ctypes.POINTER(vp)]),
     "cvx_plan_create_host": (c_status, [ctypes.POINTER(CvxHostJob), u32, u32, ctypes.POINTER(vp)]),

@@ -20,10 +20,9 @@ from ._lib import (CvxError, CvxHostJob, CvxJob, CvxServerConfig, CvxServerReque
 
 __all__ = ["VoxInfo", "voxelize", "voxelize_solid", "voxelize_ws", "workspace_size", "create_mesh_bbox_cube",
            "mesh_bbox", "make_voxinfo", "table_words", "Job", "voxelize_batch", "Plan", "HostJob", "HostPlan",
-           "device_status",
-           "get_tuning", "set_tuning", "CvxError", "voxelize_host", "profile_enable", "profile_collect", "Server",
-           "mesh_bbox_device", "voxinfo_from_device", "gather_soup", "transcode", "encode_binvox", "binvox_header",
-           "encode_voxel_list"]
+           "device_status", "get_tuning", "set_tuning", "CvxError", "stream_release", "voxelize_host",
+           "profile_enable", "profile_collect", "Server", "mesh_bbox_device", "voxinfo_from_device", "gather_soup",
+           "transcode", "encode_binvox", "binvox_header", "encode_voxel_list"]
 
 
 VoxInfo = CvxVoxinfo
@@ -118,6 +117,12 @@ def voxelize_solid(info: VoxInfo, triangle_data, vtable, morton_code: bool = Fal
     _check_sizes(info, triangle_data, vtable)
     check(lib.cvx_voxelize_solid(ctypes.byref(info), _ptr(triangle_data), _ptr(vtable), int(bool(morton_code)),
                                  _stream(stream)), "cvx_voxelize_solid")
+
+
+def stream_release(stream=None) -> None:
+    """cvx_stream_release: synchronize ``stream`` and free the scratch the library keeps for it
+    (call before destroying a stream used with the library)."""
+    check(lib.cvx_stream_release(_stream(stream)), "cvx_stream_release")
 
 
 def workspace_size(info: VoxInfo, solid: bool) -> int:

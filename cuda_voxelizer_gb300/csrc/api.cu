@@ -670,6 +670,26 @@ cvx_status cvx_device_status(cvx_stream_t stream) {
 	return CVX_OK;
 }
 
+cvx_status cvx_stream_release(cvx_stream_t stream) {
+	int dev = 0;
+	CVX_CUDA(cudaGetDevice(&dev));
+	cudaStream_t s = (cudaStream_t)stream;
+	StreamScratch w;
+	{
+		std::lock_guard<std::mutex> lk(g_mu);
+		auto it = g_ws.find({dev, s});
+		if (it == g_ws.end()) return CVX_OK;
+		w = it->second;
+		g_ws.erase(it);
+	}
+	CVX_CUDA(cudaStreamSynchronize(s));  // no kernel of the stream still uses the scratch
+	if (w.staging_done) cudaEventDestroy(w.staging_done);
+	if (w.staging) cudaFreeHost(w.staging);
+	if (w.rec) cudaFree(w.rec);
+	if (w.flips) cudaFree(w.flips);
+	return CVX_OK;
+}
+
 cvx_status cvx_voxelize_batch(const cvx_job* jobs, uint32_t n_jobs, cvx_stream_t stream) {
 	if (n_jobs && !jobs) return fail(CVX_ERR_INVALID_VALUE, "jobs is null");
 	std::vector<JobDesc> surf, solid;

@@ -112,6 +112,12 @@ cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const float* d_tr
  * library-owned scratch: CVX_OK, or CVX_ERR_DEVICE_CHECK (a queue overflow or a timed-out copy). */
 cvx_status cvx_device_status(cvx_stream_t stream);
 
+/* Synchronizes `stream` and frees the scratch the library allocated for it (on the current device).
+ * Call it before destroying a stream used with the library: a later stream can get the same handle,
+ * and would otherwise share scratch with work still running on the old one.  Calls on the stream
+ * afterwards allocate afresh; a stream the library never used returns CVX_OK at once. */
+cvx_status cvx_stream_release(cvx_stream_t stream);
+
 /* ---- batches: many meshes of different sizes, grids and modes in one launch sequence ---------- */
 
 typedef struct cvx_job {

@@ -319,6 +319,25 @@ def test_plan_equals_single_calls_and_replays():
     plan.close()
 
 
+@pytest.mark.parametrize("solid", [False, True])
+def test_stream_release_frees_scratch_and_calls_still_work(solid):
+    """cvx_stream_release frees a stream's scratch; later calls on the stream allocate it afresh
+    and give the same table."""
+    t = meshgen.icosphere(21, level=5)
+    info = info_of(t, 128)
+    td = torch.from_numpy(t.reshape(-1)).cuda()
+    s = torch.cuda.Stream()
+    tables = []
+    for _ in range(2):
+        tab = torch.zeros(cv.table_words(info) + GUARD, dtype=torch.int32, device="cuda")
+        with torch.cuda.stream(s):
+            (cv.voxelize_solid if solid else cv.voxelize)(info, td, tab, True, stream=s)
+        cv.stream_release(s)  # synchronizes the stream, then frees
+        tables.append(tab)
+    assert torch.equal(tables[0], tables[1]) and int(tables[0].count_nonzero()) > 0
+    cv.stream_release(torch.cuda.Stream())  # a stream the library never used
+
+
 def test_plan_without_clearing_keeps_xor_semantics():
     """A plan that does not clear its tables ORs (surface) and XORs (solid) into them like plain
     calls: launched twice, surface tables are unchanged and solid tables return to zero."""
