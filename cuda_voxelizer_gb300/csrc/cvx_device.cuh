@@ -35,7 +35,12 @@ struct RefFma {
 	static constexpr int edge_zx = 2;  // per-voxel dot(n_zx_e, p_zx): fma(a.y, px, a.x*pz) (pz term hoisted)
 	static constexpr int ccw = 2;      // solid checkCCW: e0.x*e1.y - e1.x*e0.y -> fma(-e1.x, e0.y, e0.x*e1.y)
 	static constexpr int pt = 1;       // solid check_point_triangle t1..t3: fma(a, b, -(c*d))
-	static constexpr int getx = 1;     // solid get_x_coordinate: fma(n.y, A, n.z*B)
+	static constexpr int getx = 1;     // solid get_x_coordinate: fma(n.y, A, n.z*B) for linear tables,
+	static constexpr int getx_morton = 2;  // fma(n.z, B, n.y*A) for Morton tables: the reference
+	                                   //   kernel tests its morton_order argument inside the x loop,
+	                                   //   and its compiled Morton copy contracts the sum the other
+	                                   //   way (xmax then differs by one voxel on a few columns, e.g.
+	                                   //   16 of ~700k on a 1024^3 soup)
 };
 
 template <int P>

@@ -124,9 +124,10 @@ __device__ __forceinline__ bool top_left(float v0x, float v0y, float v1x, float 
 	return (v1y < v0y) || (v1y == v0y && v0x > v1x);  // :67-70
 }
 
-// Column test for voxel-centre column (y, z): returns true and xmax on a hit (:119-123).
+// Column test for voxel-centre column (y, z): returns true and xmax on a hit (:119-123).  `morton`
+// selects the contraction of get_x_coordinate the reference uses for that table order.
 template <class P>
-__device__ __forceinline__ bool column_hit(const SolidTri& S, const float* unit, int y, int z, int& xmax) {
+__device__ __forceinline__ bool column_hit(const SolidTri& S, const float* unit, int y, int z, bool morton, int& xmax) {
 	// ((y + 0.5) * unit.y) in double then rounded to float == the float product of the exact y+0.5f
 	// for |y| < 2^22 (the double product is exact, so both round the same real number once).
 	const float px = __fmul_rn(__int2float_rn(y) + 0.5f, unit[1]);
@@ -148,7 +149,8 @@ __device__ __forceinline__ bool column_hit(const SolidTri& S, const float* unit,
 	                (check == 3 && top_left(S.cx, S.cy, S.ax, S.ay)) || (check == 0);
 	if (!in) return false;
 	// get_x_coordinate (:49-52): -(n.y*(p.x - v0.y) + n.z*(p.y - v0.z)) / n.x + v0.x
-	const float m = mul_add<P::getx>(S.ny, __fsub_rn(px, S.v0y), S.nz, __fsub_rn(py, S.v0z));
+	const float A = __fsub_rn(px, S.v0y), B = __fsub_rn(py, S.v0z);
+	const float m = morton ? mul_add<P::getx_morton>(S.ny, A, S.nz, B) : mul_add<P::getx>(S.ny, A, S.nz, B);
 	const float xh = __fadd_rn(__fdiv_rn(-m, S.nx), S.v0x);
 	xmax = trunc_half(__fdiv_rn(xh, unit[0]));  // int(... / unit.x - 0.5), the 0.5 a double
 	return true;
@@ -366,7 +368,7 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 		S.ax = o.ax; S.ay = o.ay; S.bx = o.bx; S.by = o.by; S.cx = o.cx; S.cy = o.cy;
 		const int y = o.y0 + (int)((it >> 8) & 0xFFu), z = o.z0 + (int)(it >> 16);
 		int xmax;
-		if (column_hit<P>(S, unit, y, z, xmax)) record_hit(flips, grid, morton, y, z, xmax);
+		if (column_hit<P>(S, unit, y, z, morton, xmax)) record_hit(flips, grid, morton, y, z, xmax);
 	}
 }
 
@@ -445,7 +447,7 @@ __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant
 				z = S.z0 + (int)(c % nzc);
 			}
 			int xmax;
-			if (column_hit<P>(S, unit, y, z, xmax)) record_hit(J.flips, grid, morton, y, z, xmax);
+			if (column_hit<P>(S, unit, y, z, morton, xmax)) record_hit(J.flips, grid, morton, y, z, xmax);
 		}
 	}
 }

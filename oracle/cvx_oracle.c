@@ -56,7 +56,8 @@ typedef struct {
     int edge_yz;    /* per-voxel dot(n_yz,p_yz): 1 = fma(a.x,py,a.y*pz), 2 = fma(a.y,pz,a.x*py) */
     int edge_zx;    /* per-voxel dot(n_zx,p_zx): 1 = fma(a.x,pz,a.y*px), 2 = fma(a.y,px,a.x*pz) */
     int ccw;        /* solid checkCCW / check_point_triangle a*b-c*d: as cross */
-    int getx;       /* solid get_x_coordinate n.y*A+n.z*B: 1 = fma(n.y,A,n.z*B), 2 = fma(n.z,B,n.y*A) */
+    int getx;       /* solid get_x_coordinate n.y*A+n.z*B: 1 = fma(n.y,A,n.z*B), 2 = fma(n.z,B,n.y*A)
+                     * (the reference GPU kernel's linear-order code uses 1, its Morton-order code 2) */
     const float* inv_len; /* optional per-triangle rsqrtf(dot(c,c)) values from the device */
 } ovx_mode;
 

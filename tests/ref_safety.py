@@ -15,9 +15,11 @@ produce such a write, using float64 geometry with generous margins:
   * triangles whose float32 cross product is exactly zero (the reference's normal is NaN, so it
     only ever writes x = 0) are kept;
   * other triangles are dropped when nearly degenerate (sine of the corner angle < 1e-3) or nearly
-    parallel to x (|n.x| < 1e-3), where float32 xmax is not predictable from float64;
+    parallel to x (|n.x| < 1e-2), where float32 xmax is not predictable from float64 (at
+    |n.x| = 0.0017 a random soup at 1024^3 gave a float32 xmax of 1056 where float64 put the plane
+    inside the grid, and the reference wrote past its table);
   * the rest are dropped if, at any column centre within 1e-3 voxel of the triangle's yz
-    projection, the plane's x (plus a 2-voxel margin) reaches g - 1 (Morton) or the run
+    projection, the plane's x (plus a 16-voxel margin) reaches g - 1 (Morton) or the run
     x + y*gx + z*gx*gy (plus margin) reaches the end of the table (linear).
 The engine itself clips these writes (x to the grid in Morton order, the run to the table in linear
 order), so it needs no such filter.
@@ -51,7 +53,7 @@ def safe_triangles(tris: np.ndarray, info_bytes: bytes, morton: bool) -> np.ndar
     sin = cn / np.maximum(np.linalg.norm(e0, axis=1) * np.linalg.norm(e1, axis=1), 1e-300)
     n = c / np.maximum(cn, 1e-300)[:, None]
     zero = _cross32_zero(t32)
-    keep = zero | ((sin >= 1e-3) & (np.abs(n[:, 0]) >= 1e-3))
+    keep = zero | ((sin >= 1e-3) & (np.abs(n[:, 0]) >= 1e-2))
     cand = np.nonzero(keep & ~zero)[0]
     # column ranges (voxel-centre columns of the yz bbox, widened by one)
     lo = np.minimum(np.minimum(v0, v1), v2)[:, 1:]
@@ -103,7 +105,7 @@ def safe_triangles(tris: np.ndarray, info_bytes: bytes, morton: bool) -> np.ndar
         hit = valid & (inside | near)
         nn = n[idx]
         xh = -(nn[:, 1:2] * (py - v0[idx][:, 1:2]) + nn[:, 2:3] * (pz - v0[idx][:, 2:3])) / nn[:, 0:1] + v0[idx][:, 0:1]
-        xmax = xh / unit[0] - 0.5 + 2.0
+        xmax = xh / unit[0] - 0.5 + 16.0
         if morton:
             over = hit & (xmax >= g[0] - 1)
         else:

@@ -197,6 +197,26 @@ def test_grid_2048_indices_above_32_bits(ref, morton):
     assert differ == 0 and set_words > 0, f"{differ} words differ"
 
 
+@pytest.mark.parametrize("morton", [False, True])
+def test_solid_1024_large_triangles_both_orders(ref, morton):
+    """A 1024^3 soup of large triangles, solid, in both orders.  The reference kernel contracts
+    get_x_coordinate differently in its linear and Morton code (fma on the n.y term, on the n.z
+    term), so on a few columns of this mesh its xmax differs by one voxel between the two orders;
+    the engine follows each order."""
+    t = meshgen.soup(616136667, n=35380, lmin=0.3 / 1024, lmax=200 / 1024).astype(np.float32)
+    info = info_of(t, 1024)
+    t, info = for_reference(t, info, morton, True)
+    d = torch.from_numpy(np.ascontiguousarray(t).reshape(-1)).cuda()
+    a = run_engine(info, d, morton, True)
+    b = run_ref(ref, info, d, morton, True)
+    torch.cuda.synchronize()
+    cv.device_status()
+    differ, set_words = int((a != b).sum()), int(a.count_nonzero())
+    del a, b
+    torch.cuda.empty_cache()
+    assert differ == 0 and set_words > 0, f"{differ} words differ"
+
+
 def test_linear_grid_of_exactly_2_to_32_voxels(ref):
     """2048 x 2048 x 1024: the largest linear index is 2^32 - 1, the edge of the 32-bit path."""
     t = np.concatenate([meshgen.soup(9, n=30_000, lmin=0.3 / 2048, lmax=8 / 2048),
