@@ -669,7 +669,9 @@ cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint
 	std::string first_msg;
 	for (uint32_t i = 0; i < n; i++) {
 		const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
-		if (due - Clock::now() > std::chrono::microseconds(300)) std::this_thread::sleep_until(due - std::chrono::microseconds(200));
+		// sleep to 50 us before the arrival, then spin: a generator that spins longer keeps a whole
+		// core busy at high rates and competes with the server's own threads
+		if (due - Clock::now() > std::chrono::microseconds(100)) std::this_thread::sleep_until(due - std::chrono::microseconds(50));
 		Clock::time_point now;
 		while ((now = Clock::now()) < due) {
 		}

@@ -163,6 +163,48 @@ def test_adversarial_vs_reference_kernels(ref, g, morton, solid):
     assert_same(a, b, f"adversarial g={g}")
 
 
+def _random_case(seed):
+    """One seeded random configuration: grid (cubic or not, 8 to 1024), mode, soup size and
+    triangle-size range."""
+    rng = np.random.default_rng(seed)
+    cubic = rng.random() < 0.7
+    g = int(rng.choice([8, 16, 32, 37, 64, 100, 128, 256, 512, 1024])) if cubic else None
+    dims = (g, g, g) if cubic else tuple(int(x) for x in rng.integers(5, 300, 3))
+    morton = bool(cubic and (g & (g - 1)) == 0 and rng.random() < 0.5)
+    solid = bool(rng.random() < 0.5)
+    gm = max(dims)
+    t = meshgen.soup(int(rng.integers(1 << 30)), n=int(rng.integers(1, 40000)), lmin=0.3 / gm,
+                     lmax=float(rng.choice([2, 8, 40, 200])) / gm).astype(np.float32)
+    info = info_of(t, dims[0])
+    for i in range(3):
+        info.gridsize[i] = dims[i]
+        info.unit[i] = np.float32((np.float32(info.bbox_max[i]) - np.float32(info.bbox_min[i])) / np.float32(dims[i]))
+    return t, info, morton, solid
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_randomized_vs_reference_kernels(ref, seed):
+    """Seeded random soups, grids and modes: per call and as a clearing plan over a dirty table,
+    against the reference kernels (a sweep like this found the per-order contraction of
+    get_x_coordinate)."""
+    t, info, morton, solid = _random_case(1000 + seed)
+    t, info = for_reference(t, info, morton, solid)
+    d = torch.from_numpy(np.ascontiguousarray(t).reshape(-1)).cuda()
+    W = cv.table_words(info)
+    a = run_engine(info, d, morton, solid)
+    b = run_ref(ref, info, d, morton, solid)
+    c = torch.full((W + GUARD,), 0x5A5A5A5A, dtype=torch.int32, device="cuda")
+    c[W:] = 0
+    plan = cv.Plan([cv.Job(info, d, c, morton, solid)], clear_tables=True)
+    plan.launch()
+    torch.cuda.synchronize()
+    cv.device_status()
+    plan.close()
+    dims = tuple(info.gridsize)
+    assert torch.equal(a, b), f"{dims} morton={morton} solid={solid}: {int((a != b).sum())} words differ (call)"
+    assert torch.equal(c, b), f"{dims} morton={morton} solid={solid}: {int((c != b).sum())} words differ (plan)"
+
+
 @pytest.mark.parametrize("solid", [False, True])
 def test_non_cubic_grid(ref, solid):
     t = meshgen.icosphere(4, level=4)
