@@ -9,13 +9,15 @@
 // XORs the resolved bits into the caller's table (or scatters them into Morton order).  The XOR of
 // any set of [0, xmax] ranges is exactly what this produces.
 //
-// Kernels, in launch order:
+// Kernels, in launch order (each after the first launched with launch_after, waiting on its
+// predecessor with pdl_wait):
 //   solid_classify      one CTA per 256-triangle tile (TMA bulk staging as in surface.cu); the
 //                       columns of triangles with at most `small_cols` columns are dealt over the
 //                       CTA, the other triangles queued.
 //   solid_cols          persistent; each warp takes items of up to kColsPerItem columns.
-//   solid_resolve       one thread per row run (whole rows; 16-byte words where rows are aligned):
-//                       prefix XOR along x, XORed into the linear table, flip table cleared.
+//   solid_resolve       linear jobs: one thread per row run (whole rows; 16-byte words where rows
+//                       are aligned): prefix XOR along x, XORed into the linear table (stored, for
+//                       JOB_TABLE_ZERO jobs), flip table cleared.
 //   solid_morton_slab   Morton jobs with 32 <= g <= 1024: a CTA resolves a 16 x 16-row slab in
 //                       shared memory and writes it as 16^3 Morton blocks (128 contiguous words).
 //   solid_morton_brick  Morton jobs with g > 1024: groups of x-adjacent 32^3 bricks.

@@ -6,13 +6,17 @@
 //                  memory with one cp.async.bulk (TMA bulk copy) when it is full and 16-byte
 //                  aligned.  Each thread sets up its triangle; triangles whose grid bbox holds at
 //                  most `small_vox` voxels (every voxel tested, like the reference) or at most
-//                  kLocalRows rows (row intervals) are finished by the CTA, their rows dealt over
+//                  kLocalRows rows (rows of up to kMaskRowVoxels voxels tested voxel by voxel,
+//                  longer rows by row intervals) are finished by the CTA, their rows dealt over
 //                  its threads; the others are queued, one record per triangle, as one item
 //                  ("mid") or as one item per 32 z-slices ("big").
-//   surf_rows      persistent CTAs; each warp takes work tickets (big items first, then mid
-//                  triangles), finds the y-interval of every z-slice of the item (one lane per
-//                  slice), flattens the (y, z) rows and gives one row per lane; each lane finds the
-//                  exact x-interval of its row and ORs it into the table one word at a time.
+//   surf_rows      persistent CTAs, launched with launch_after (pdl_wait before reading the
+//                  queue); each warp takes work tickets (big items first, then mid triangles),
+//                  finds the y-interval of every z-slice of the item (one lane per slice),
+//                  flattens the (y, z) rows and gives one row per lane; each lane finds the exact
+//                  x-interval of its row and ORs it into the table one word at a time (the whole
+//                  warp for long rows).  Jobs whose indices fit 32 bits (JOB_NARROW) write with
+//                  32-bit index arithmetic.
 #include "engine.h"
 #include "surface.cuh"
 
