@@ -18,8 +18,9 @@ produce such a write, using float64 geometry with generous margins:
     parallel to x (|n.x| < 1e-2), where float32 xmax is not predictable from float64 (at
     |n.x| = 0.0017 a random soup at 1024^3 gave a float32 xmax of 1056 where float64 put the plane
     inside the grid, and the reference wrote past its table);
-  * the rest are dropped if, at any column centre within 1e-3 voxel of the triangle's yz
-    projection, the plane's x (plus a 16-voxel margin) reaches g - 1 (Morton) or the run
+  * the rest are dropped if, at any column centre the reference can count as a hit (inside the
+    triangle's yz projection or within 1e-3 world units of an edge: the reference's 1e-6 tolerance
+    on an edge's cross product), the plane's x (plus a 16-voxel margin) reaches g - 1 (Morton) or the run
     x + y*gx + z*gx*gy (plus margin) reaches the end of the table (linear).
 The engine itself clips these writes (x to the grid in Morton order, the run to the table in linear
 order), so it needs no such filter.
@@ -64,7 +65,10 @@ def safe_triangles(tris: np.ndarray, info_bytes: bytes, morton: bool) -> np.ndar
     z1 = np.floor(hi[:, 1] / unit[2] - 0.5).astype(np.int64) + 1
     ny_cols = np.maximum(y1 - y0 + 1, 0)
     nz_cols = np.maximum(z1 - z0 + 1, 0)
-    tol = 1e-3 * float(min(unit[1], unit[2]))
+    # The reference accepts a column "on" an edge when |cross(PA, PB)| < 1e-6 (world units squared)
+    # and the column centre lies within the edge's bounding box: up to min(L, 1e-6 / L) <= 1e-3
+    # world units from an edge of length L.  Columns that close to the projection count as hits.
+    tol = max(1e-3 * float(min(unit[1], unit[2])), 1e-3)
     bad = np.zeros(t.shape[0], dtype=bool)
     # process triangles in groups of equal column-count bound to stay vectorised
     cols = ny_cols * nz_cols
