@@ -259,6 +259,44 @@ def test_solid_1024_large_triangles_both_orders(ref, morton):
     assert differ == 0 and set_words > 0, f"{differ} words differ"
 
 
+def _near_x_parallel(seed, n, g):
+    """Triangles whose planes are nearly parallel to x (|n.x| log-uniform in [1e-5, 1e-2]), every
+    vertex in z <= 0.45 of a unit-cube grid box."""
+    rng = np.random.default_rng(seed)
+    c = np.stack([rng.uniform(0.05, 0.95, n), rng.uniform(0.05, 0.95, n), rng.uniform(0.05, 0.40, n)], 1)
+    size = np.exp(rng.uniform(np.log(0.5 / g), np.log(40 / g), n))
+    nx = np.exp(rng.uniform(np.log(1e-5), np.log(1e-2), n)) * rng.choice([-1, 1], n)
+    phi = rng.uniform(0, 2 * np.pi, n)
+    nrm = np.stack([nx, np.sqrt(1 - nx * nx) * np.cos(phi), np.sqrt(1 - nx * nx) * np.sin(phi)], 1)
+    a = np.cross(nrm, np.array([1.0, 0, 0]))
+    a /= np.linalg.norm(a, axis=1)[:, None]
+    b = np.cross(nrm, a)
+    ang = rng.uniform(0, 2 * np.pi, (n, 3)) + np.array([0, 2.1, 4.2])
+    v = c[:, None, :] + size[:, None, None] * (np.cos(ang)[..., None] * a[:, None, :] + np.sin(ang)[..., None] * b[:, None, :])
+    v[..., 2] = np.clip(v[..., 2], 0.0, 0.45)
+    v[..., :2] = np.clip(v[..., :2], 0.0, 1.0)
+    return v.reshape(n, 9).astype(np.float32)
+
+
+@pytest.mark.parametrize("g", [512, 1024])
+def test_near_x_parallel_solid_linear(ref, g):
+    """Solid voxelization where xmax is most sensitive to float32 rounding (|n.x| down to 1e-5,
+    which the reference-safety filter drops elsewhere).  Safe for the reference kernel by
+    construction: every triangle lies in z <= 0.45 of the grid, so a run past x = gx continues
+    into following rows of the same table (more than g^2 / 2 rows follow any hit column)."""
+    t = _near_x_parallel(100 * g, 20000, g)
+    info = cv.make_info((0, 0, 0), (1, 1, 1), g, t.shape[0])
+    d = torch.from_numpy(t.reshape(-1).copy()).cuda()
+    a = run_engine(info, d, False, True)
+    b = run_ref(ref, info, d, False, True)
+    torch.cuda.synchronize()
+    cv.device_status()
+    differ = int((a != b).sum())
+    del a, b
+    torch.cuda.empty_cache()
+    assert differ == 0, f"{differ} words differ"
+
+
 def test_linear_grid_of_exactly_2_to_32_voxels(ref):
     """2048 x 2048 x 1024: the largest linear index is 2^32 - 1, the edge of the 32-bit path."""
     t = np.concatenate([meshgen.soup(9, n=30_000, lmin=0.3 / 2048, lmax=8 / 2048),
