@@ -223,6 +223,7 @@ JobDesc make_job(const cvx_voxinfo& v, const float* tris, uint32_t* table, int m
 	j.flags = (morton ? JOB_MORTON : 0u) | (solid ? JOB_SOLID : 0u);
 	const uint64_t voxels = (uint64_t)v.gridsize[0] * v.gridsize[1] * v.gridsize[2];
 	if (morton ? v.gridsize[0] <= 1024 : voxels <= (1ull << 32)) j.flags |= JOB_NARROW;
+	if (v.n_triangles && needs_plain_loads(tris)) j.flags |= JOB_PLAIN_LOADS;
 	return j;
 }
 
@@ -507,6 +508,20 @@ cvx_status cvx::run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* con
 
 void cvx::set_message(const std::string& m) { g_msg = m; }
 
+bool cvx::needs_plain_loads(const void* p) {
+	if (!p) return false;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return true;
+	}
+	return a.type != cudaMemoryTypeDevice;
+}
+
+cvx_status cvx::validate_call(const cvx_voxinfo* info, const void* tris, const void* table, int morton) {
+	return validate(info, tris, table, morton);
+}
+
 // ==== C ABI =======================================================================================
 
 extern "C" {
@@ -661,12 +676,19 @@ cvx_status cvx_device_status(cvx_stream_t stream) {
 	{
 		std::lock_guard<std::mutex> lk(g_mu);
 		auto it = g_ws.find({dev, s});
-		if (it == g_ws.end()) return CVX_OK;
-		rec = it->second.rec;
+		if (it != g_ws.end()) rec = it->second.rec;
 	}
-	Counters c;
-	CVX_CUDA(cudaMemcpy(&c, rec, sizeof(c), cudaMemcpyDeviceToHost));
-	if (c.error) return fail(CVX_ERR_DEVICE_CHECK, "device check failed (code %u)", c.error);
+	if (rec) {
+		Counters c;
+		CVX_CUDA(cudaMemcpy(&c, rec, sizeof(c), cudaMemcpyDeviceToHost));
+		if (c.error) return fail(CVX_ERR_DEVICE_CHECK, "device check failed (code %u)", c.error);
+	}
+	// the last cvx_voxelize_solid_noalloc call on this device keeps its counters in the library's
+	// fixed scratch array
+	unsigned err = 0;
+	cvx_status st = noalloc_error(dev, &err);
+	if (st != CVX_OK) return st;
+	if (err) return fail(CVX_ERR_DEVICE_CHECK, "device check failed in cvx_voxelize_solid_noalloc (code %u)", err);
 	return CVX_OK;
 }
 

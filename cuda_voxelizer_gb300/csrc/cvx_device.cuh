@@ -71,7 +71,10 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 // JOB_TABLE_ZERO: the engine zeroed the job's table earlier in the same launch sequence (plans that
 // clear their tables, host plans, server batches), so the solid passes store their words instead of
 // XOR-ing them into the table (same result, no read) and skip words that resolve to zero.
-enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u, JOB_TABLE_ZERO = 8u };
+// JOB_PLAIN_LOADS: the job's triangles are not plain device memory (managed, host-registered or
+// system memory -- the reference's main() passes cudaMallocManaged buffers): the classify kernels
+// read them with ordinary loads instead of bulk copies.
+enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u, JOB_TABLE_ZERO = 8u, JOB_PLAIN_LOADS = 16u };
 
 // One mesh voxelization.  Plain data, uploaded as an array for batches or passed by value for a
 // single mesh.

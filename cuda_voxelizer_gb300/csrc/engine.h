@@ -94,6 +94,19 @@ cudaError_t launch_clear(const ClearRange* d_ranges, uint32_t n, uint32_t total_
 // Sets the message returned by cvx_last_error_message() on this host thread.
 void set_message(const std::string& m);
 
+// The argument checks of cvx_voxelize / cvx_voxelize_solid (null pointers, zero or oversized grid
+// axes, Morton order on a grid it cannot address); sets the message on failure.
+cvx_status validate_call(const cvx_voxinfo* info, const void* tris, const void* table, int morton);
+
+// True unless `p` is known to be plain device memory (cudaMalloc, a memory pool, a VMM mapping).
+// Managed, host-registered and system memory are read with ordinary loads (JOB_PLAIN_LOADS): the
+// load instructions handle their page faults and migrations.
+bool needs_plain_loads(const void* p);
+
+// Error word left by the last cvx_voxelize_solid_noalloc call on device `dev` in the library's fixed
+// scratch array (0 if there was none).  The caller has synchronized the stream of that call.
+cvx_status noalloc_error(int dev, unsigned* err);
+
 // A batch run on caller-owned memory (used by the server, whose memory all comes from its budget).
 // batch_scratch_bytes gives the device record bytes (256-byte aligned) and the pinned host staging
 // bytes that run_batch_on needs for `jobs`.  run_batch_on takes one flip table per job in `flips`

@@ -14,10 +14,14 @@
 //
 // Host code must not use the array's name as a device address (on the host it only names a
 // stand-in): the first call on each device looks up the real address with cudaGetSymbolAddress,
-// with that device current, and caches it.  That first call should therefore come before any
-// stream capture.  Every call shares the one array: calls that overlap on the GPU (two streams, or
-// two host threads) race on it and corrupt each other's results; issue them one after another.
-// Each call clears the parts that must start at zero (counters, the flip table of its grid).
+// with that device current, and caches it together with the id of the CUDA context it belongs to.
+// That first call should therefore come before any stream capture.  A later call from another
+// context (after cudaDeviceReset, or after the primary context was released and made again) sees
+// the id change and looks the address up afresh.  Every call shares the one array: calls that
+// overlap on the GPU (two streams, or two host threads) race on it and corrupt each other's
+// results; issue them one after another.  Each call clears the parts that must start at zero
+// (counters, the flip table of its grid).  cvx_device_status reports the device-side checks of the
+// last call on the current device (its error word lives in the array too).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -43,14 +47,53 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratch
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
 int g_cols_grid[kMaxDevices] = {};
 
-// Device address of the scratch array for the current device (looked up once per device).
+// Id of the current CUDA context (cuCtxGetCurrent + cuCtxGetId, reached through the runtime so the
+// library needs no link dependency on the driver library).  Ids are unique within the process.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+cvx_status current_context_id(unsigned long long* id) {
+	static CtxGetCurrentFn get_current = nullptr;
+	static CtxGetIdFn get_id = nullptr;
+	if (!get_current || !get_id) {
+		void* f0 = nullptr;
+		void* f1 = nullptr;
+		cudaDriverEntryPointQueryResult q0, q1;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+		    cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+		    q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1) {
+			cudaGetLastError();
+			set_message("cvx_voxelize_solid_noalloc: cuCtxGetCurrent/cuCtxGetId not available");
+			return CVX_ERR_CUDA;
+		}
+		get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+		get_id = reinterpret_cast<CtxGetIdFn>(f1);
+	}
+	void* ctx = nullptr;
+	if (get_current(&ctx) != 0 || !ctx || get_id(ctx, id) != 0) {
+		set_message("cvx_voxelize_solid_noalloc: no current CUDA context");
+		return CVX_ERR_CUDA;
+	}
+	return CVX_OK;
+}
+
+// Device address of the scratch array for the current device and context (looked up once per
+// context).
 cvx_status scratch_address(int dev, void** out, int* cols_grid) {
+	cudaError_t e = cudaSetDevice(dev);  // makes the device's primary context current (no allocation)
+	if (e != cudaSuccess) {
+		set_message(std::string("cvx_voxelize_solid_noalloc: cannot initialise the device: ") + cudaGetErrorString(e));
+		return CVX_ERR_CUDA;
+	}
+	unsigned long long ctx = 0;
+	cvx_status st = current_context_id(&ctx);
+	if (st != CVX_OK) return st;
 	std::lock_guard<std::mutex> lk(g_mu);
-	if (!g_addr[dev]) {
+	if (!g_addr[dev] || g_ctx_id[dev] != ctx) {
 		void* p = nullptr;
-		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
 		if (e != cudaSuccess || p == nullptr) {
 			set_message(std::string("cudaGetSymbolAddress(noalloc scratch): ") + cudaGetErrorString(e));
 			return CVX_ERR_CUDA;
@@ -63,6 +106,7 @@ cvx_status scratch_address(int dev, void** out, int* cols_grid) {
 		}
 		g_cols_grid[dev] = sms * solid_cols_blocks_per_sm();
 		g_addr[dev] = p;
+		g_ctx_id[dev] = ctx;
 	}
 	*out = g_addr[dev];
 	*cols_grid = g_cols_grid[dev];
@@ -76,21 +120,40 @@ cvx_status cuda_status(cudaError_t e, const char* what) {
 }
 
 }  // namespace
+
+cvx_status noalloc_error(int dev, unsigned* err) {
+	*err = 0;
+	if (dev < 0 || dev >= kMaxDevices) return CVX_OK;
+	void* base = nullptr;
+	{
+		std::lock_guard<std::mutex> lk(g_mu);
+		if (!g_addr[dev]) return CVX_OK;  // no call on this device yet
+		unsigned long long ctx = 0;
+		if (current_context_id(&ctx) != CVX_OK || ctx != g_ctx_id[dev]) return CVX_OK;  // none in this context
+		base = g_addr[dev];
+	}
+	Counters c;
+	cudaError_t e = cudaMemcpy(&c, base, sizeof(c), cudaMemcpyDeviceToHost);
+	if (e != cudaSuccess) {
+		set_message(std::string("cudaMemcpy(noalloc counters): ") + cudaGetErrorString(e));
+		return CVX_ERR_CUDA;
+	}
+	*err = c.error;
+	return CVX_OK;
+}
+
 }  // namespace cvx
 
 using namespace cvx;
 
 extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const float* d_triangles, uint32_t* d_table,
                                                  int morton, cvx_stream_t stream) {
-	if (!info || !d_table || (info->n_triangles && !d_triangles)) {
-		set_message("cvx_voxelize_solid_noalloc: null argument");
-		return CVX_ERR_INVALID_VALUE;
-	}
+	// the checks of cvx_voxelize_solid: null pointers, zero axes, axes above 2^22 (the solid
+	// column arithmetic reproduces the reference only below that), Morton order on grids it cannot
+	// address
+	cvx_status st = validate_call(info, d_triangles, d_table, morton);
+	if (st != CVX_OK) return st;
 	const uint64_t g0 = info->gridsize[0], g1 = info->gridsize[1], g2 = info->gridsize[2];
-	if (!g0 || !g1 || !g2) {
-		set_message("cvx_voxelize_solid_noalloc: gridsize has a zero dimension");
-		return CVX_ERR_INVALID_VALUE;
-	}
 	if (g0 * g1 * g2 > kNoallocMaxVoxels) {
 		char buf[256];
 		std::snprintf(buf, sizeof(buf),
@@ -101,13 +164,9 @@ extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const 
 		set_message(buf);
 		return CVX_ERR_INVALID_VALUE;
 	}
-	if (morton && (g0 != g1 || g1 != g2 || (g0 & (g0 - 1)))) {
-		set_message("cvx_voxelize_solid_noalloc: Morton order needs a cubic power-of-two grid");
-		return CVX_ERR_UNSUPPORTED;
-	}
 	if (info->n_triangles == 0) return CVX_OK;
 	int dev = 0;
-	cvx_status st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+	st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
 	if (st != CVX_OK) return st;
 	if (dev < 0 || dev >= kMaxDevices) {
 		set_message("cvx_voxelize_solid_noalloc: device index out of range");
@@ -141,7 +200,7 @@ extern "C" cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const 
 		job.inv_unit[i] = one / info->unit[i];
 		job.grid[i] = info->gridsize[i];
 	}
-	job.flags = (morton ? JOB_MORTON : 0u) | JOB_SOLID;
+	job.flags = (morton ? JOB_MORTON : 0u) | JOB_SOLID | (needs_plain_loads(d_triangles) ? JOB_PLAIN_LOADS : 0u);
 	const SolidUnits su = solid_units(job.grid);
 
 	LaunchDesc L{};

@@ -43,11 +43,15 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Stage `cnt` triangles (9 floats each) from global memory into shared memory.  A full, aligned
-// tile goes through one bulk copy completing on an mbarrier; anything else is loaded cooperatively.
-__device__ __forceinline__ void stage_tile(const LaunchDesc& L, const float* src, uint32_t cnt, float* s_tri,
-                                           uint64_t* s_bar) {
+// tile of plain device memory goes through one bulk copy completing on an mbarrier; anything else
+// (a partial or unaligned tile, managed or host memory: `plain`) is loaded cooperatively.
+// Returns false (in every thread) if the bulk copy did not complete within the bounded wait: the
+// error word is set, the CTA waits once more (again bounded) for the copy still in flight, and the
+// caller skips the tile without touching the shared memory the copy may still write.
+__device__ __forceinline__ bool stage_tile(const LaunchDesc& L, const float* src, uint32_t cnt, float* s_tri,
+                                           uint64_t* s_bar, bool plain) {
 	const uint32_t bytes = cnt * 36u;
-	const bool bulk = cnt == kTile && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0);
+	const bool bulk = cnt == kTile && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && !plain;
 	if (bulk) {
 		const uint32_t bar = (uint32_t)__cvta_generic_to_shared(s_bar);
 		const uint32_t dst = (uint32_t)__cvta_generic_to_shared(s_tri);
@@ -60,16 +64,17 @@ __device__ __forceinline__ void stage_tile(const LaunchDesc& L, const float* src
 			             : "memory");
 		}
 		__syncthreads();  // barrier initialised before anyone waits on it
-		if (!mbar_wait(bar, 0)) {
-			// The copy did not land in time: flag it and read the tile directly instead.  The
-			// bulk copy writes the same bytes whenever it completes.
-			set_error(L, kErrBulkTimeout);
-			for (uint32_t i = threadIdx.x; i < cnt * 9u; i += blockDim.x) s_tri[i] = src[i];
+		const bool late = !mbar_wait(bar, 0);
+		if (__syncthreads_or(late)) {
+			if (threadIdx.x == 0) set_error(L, kErrBulkTimeout);
+			mbar_wait(bar, 0);
+			return false;
 		}
-	} else {
-		for (uint32_t i = threadIdx.x; i < cnt * 9u; i += blockDim.x) s_tri[i] = src[i];
+		return true;
 	}
+	for (uint32_t i = threadIdx.x; i < cnt * 9u; i += blockDim.x) s_tri[i] = src[i];
 	__syncthreads();
+	return true;
 }
 
 // Exclusive prefix sum over the CTA (kTile threads); returns this thread's offset, total in *total.
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 	const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
 	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
 	const uint32_t cnt = (uint32_t)umin64((uint64_t)kTile, n - t0);
-	stage_tile(L, tris + t0 * 9, cnt, sm.tri, &s_bar);
+	if (!stage_tile(L, tris + t0 * 9, cnt, sm.tri, &s_bar, (J.flags & JOB_PLAIN_LOADS) != 0)) return;  // tile not staged: error word set
 
 	const uint32_t lane = threadIdx.x & 31u;
 	const bool valid = threadIdx.x < cnt;

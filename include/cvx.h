@@ -101,15 +101,19 @@ cvx_status cvx_voxelize_ws(const cvx_voxinfo* info, const float* d_triangles, ui
  * start-up (an allocation mid-frame can stall the device or fail under memory pressure), or hosts
  * whose memory policy forbids driver allocations.  Same result as cvx_voxelize_solid.  Its scratch
  * is a fixed 4 MiB array inside the library (held by every GPU that loads it until exit), so the
- * grid may hold at most 2^24 voxels (e.g. 256^3); larger grids return CVX_ERR_INVALID_VALUE.  The
- * first call on a device looks up that array's device address and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race, so issue them one at a
- * time. */
+ * grid may hold at most 2^24 voxels (e.g. 256^3); larger grids return CVX_ERR_INVALID_VALUE, and
+ * the other argument checks are those of cvx_voxelize_solid (axes up to 2^22).  The first call on a
+ * device (and in each new CUDA context of it, e.g. after cudaDeviceReset) looks up that array's
+ * device address and should come before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race, so issue them one at a time.  Device-side checks of the last call are
+ * reported by cvx_device_status (pass the stream the call ran on). */
 cvx_status cvx_voxelize_solid_noalloc(const cvx_voxinfo* info, const float* d_triangles, uint32_t* d_table,
                                       int morton, cvx_stream_t stream);
 
 /* Synchronizes `stream` and reports device-side checks of the last calls made on it through the
- * library-owned scratch: CVX_OK, or CVX_ERR_DEVICE_CHECK (a queue overflow or a timed-out copy). */
+ * library-owned scratch, and of the last cvx_voxelize_solid_noalloc call on the current device:
+ * CVX_OK, or CVX_ERR_DEVICE_CHECK (a queue overflow or a timed-out copy; the call's table is then
+ * incomplete). */
 cvx_status cvx_device_status(cvx_stream_t stream);
 
 /* Synchronizes `stream` and frees the scratch the library allocated for it (on the current device).

@@ -29,8 +29,34 @@ class OvxMode(ctypes.Structure):
 
     _fields_ = [("cross", ctypes.c_int), ("dot3", ctypes.c_int), ("dot2", ctypes.c_int),
                 ("plane", ctypes.c_int), ("edge_xy", ctypes.c_int), ("edge_yz", ctypes.c_int),
-                ("edge_zx", ctypes.c_int), ("ccw", ctypes.c_int), ("getx", ctypes.c_int),
-                ("inv_len", ctypes.POINTER(ctypes.c_float))]
+                ("edge_zx", ctypes.c_int), ("ccw", ctypes.c_int), ("pt", ctypes.c_int), ("getx", ctypes.c_int),
+                ("clip", ctypes.c_int), ("inv_len", ctypes.POINTER(ctypes.c_float))]
+
+
+def gpu_mode(morton: bool, inv_len: np.ndarray | None = None, clip: bool = True) -> OvxMode:
+    """The reference CUDA kernels' arithmetic: the fused-multiply-add pattern nvcc gives their
+    helper_math expressions on sm_103a (src/voxelize.cu:89-165, src/voxelize_solid.cu:24-64, with
+    get_x_coordinate contracted one way in the kernel's linear-order code and the other way in its
+    Morton-order code), their double-promoted solid arithmetic, and -- if given -- 1/|n| values taken
+    from the device's own rsqrtf (see :func:`device_inv_len`).  ``clip`` keeps the solid writes inside
+    the grid the way the CUDA engine does where the reference writes outside its table.  Keep the
+    ``inv_len`` array alive while the mode is in use."""
+    m = OvxMode(cross=1, dot3=1, dot2=2, plane=2, edge_xy=1, edge_yz=1, edge_zx=2, ccw=2, pt=1,
+                getx=2 if morton else 1, clip=int(bool(clip)))
+    if inv_len is not None:
+        assert inv_len.dtype == np.float32 and inv_len.flags.c_contiguous
+        m.inv_len = inv_len.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    return m
+
+
+def len2(info: bytes, tris, mode: OvxMode | None = None) -> np.ndarray:
+    """dot(c, c) of every triangle's cross product under ``mode``'s patterns (the rsqrtf argument
+    of the reference kernels' normalize)."""
+    t = _soup(tris, info)
+    ib = ctypes.create_string_buffer(bytes(info), 64)
+    out = np.zeros(t.shape[0], dtype=np.float32)
+    lib().ovx_len2(ctypes.addressof(ib), _ptr(t), ctypes.addressof(mode) if mode is not None else None, _ptr(out))
+    return out
 
 
 _lib = None
@@ -53,6 +79,7 @@ def lib():
         L.ovx_info_init.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_uint64]
         L.ovx_max_threads.restype = ctypes.c_int
+        L.ovx_len2.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.ovx_count_atomics.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         L.ovx_count_atomics.restype = ctypes.c_uint64
         L.ovx_binvox_payload.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
@@ -226,9 +253,15 @@ class RefGPU:
         L.refgpu_voxelize.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_void_p]
         L.refgpu_last_error.restype = ctypes.c_char_p
+        L.refgpu_rsqrt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]
         if L.refgpu_init(REF_DIR.encode()) != 0:
             raise RuntimeError("refgpu_init: " + L.refgpu_last_error().decode())
         self.L = L
+
+    def rsqrt(self, d_in: int, d_out: int, n: int, stream: int = 0):
+        """d_out[i] = rsqrtf(d_in[i]) on the device (float32 device buffers of n values)."""
+        if self.L.refgpu_rsqrt(d_in, d_out, n, stream) != 0:
+            raise RuntimeError("refgpu_rsqrt: " + self.L.refgpu_last_error().decode())
 
     def voxelize(self, info: bytes, d_tris: int, d_table: int, morton: bool, solid: bool, stream: int = 0):
         ib = ctypes.create_string_buffer(bytes(info), 64)

@@ -4,9 +4,13 @@
   whichever machine runs the tests).  ``-ffp-contract=off`` keeps every ``a*b+c`` a separate
   multiply and add, which is what the reference CPU build does on x86-64; without it gcc fuses
   them on aarch64 and the restatement would no longer reproduce the reference bit for bit.
-* ``oracle/_ref/``: the reference's own code, built from its sources by ``oracle/build_ref.sh``
-  when the reference tree is present (only on the development machine; elsewhere the prebuilt
-  device-code files in ``oracle/_ref`` are used as they are).
+* ``oracle/_ref/``: the reference's own code, built by ``oracle/build_ref.sh``.  Where the reference
+  tree is present (the development machine) the script stages the reference CPU voxelizer's source
+  files into ``oracle/_ref/src`` and builds everything from the tree; elsewhere (the GPU machine, which
+  receives ``oracle/_ref`` with the repository snapshot) it builds ``libref_cpu.so`` from the staged
+  sources, and the prebuilt device-code files are used as they are.  The reference tree is found
+  through the ``CVX_REFERENCE_ROOT`` environment variable, else as a checkout named ``reference``
+  next to this repository.
 * ``oracle/_build/libref_gpu_runner.so``: ``oracle/ref_gpu_runner.cu``, the driver-API loader
   that runs the reference's kernels from ``oracle/_ref/*.cubin`` (only where nvcc exists).
 """
@@ -20,7 +24,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("CVX_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("CVX_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                      "reference")
 
 
 def _run(cmd):
@@ -56,9 +61,15 @@ def build_oracle() -> str:
 
 
 def build_reference() -> None:
-    """Compile the reference's code into oracle/_ref when its sources are present."""
+    """Compile the reference's code into oracle/_ref: from the reference tree when it is present,
+    else the CPU voxelizer from the sources staged in oracle/_ref/src (when its build is missing or
+    was made for another CPU architecture)."""
     if os.path.isfile(os.path.join(REFERENCE_ROOT, "src", "cpu_voxelizer.cpp")):
         _run(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
+        return
+    staged = os.path.join(REF_OUT, "src", "cpu_voxelizer.cpp")
+    if os.path.isfile(staged) and _stale(os.path.join(REF_OUT, "libref_cpu.so"), staged):
+        _run(["bash", os.path.join(HERE, "build_ref.sh"), "--staged"])
 
 
 def build_gpu_runner() -> str | None:

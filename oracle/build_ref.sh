@@ -1,13 +1,17 @@
 #!/usr/bin/env bash
-# Build the reference's own voxelizer code, from its sources where they lie, into oracle/_ref/.
-# Test infrastructure only: these builds are the checker and the timed reference baseline,
-# never part of the product.  Nothing is copied out of the reference tree; outputs go only
-# into oracle/_ref/ (git-ignored, shipped to the GPU machine with the repository snapshot).
+# Build the reference's own voxelizer code into oracle/_ref/.
+# Test infrastructure only: these builds are the checker and the timed reference baseline, never
+# part of the product.  Outputs go only into oracle/_ref/ (git-ignored, shipped to the GPU machine
+# with the repository snapshot); nothing of the reference is committed.
 #
+#   src/                      the reference CPU voxelizer's own source files, staged unmodified from
+#                             the reference tree (src/cpu_voxelizer.{cpp,h}, util.h, timer.h,
+#                             morton_LUTs.h, libs/cuda/helper_math.h) so that machines without the
+#                             reference tree (the Arm GPU host) can build it too
 #   libref_cpu.so             src/cpu_voxelizer.cpp (OpenMP CPU voxelizer) + oracle/ref_cpu_shim.cpp,
-#                             host-architecture code, so it is only usable where it was built.
+#                             compiled from the staged copy for the machine that runs this script
 #   libref_io.so              src/util_io.cpp (output writers) + VoxWriter + oracle/ref_io_shim.cpp,
-#                             host-architecture code (golden-file generation)
+#                             host code (golden-file generation; only where the reference tree is)
 #   ref_voxelize.cubin        src/voxelize.cu        (kernel voxelize_triangle) for sm_103a
 #   ref_voxelize_solid.cubin  src/voxelize_solid.cu  (kernel voxelize_triangle_solid) for sm_103a
 #
@@ -16,25 +20,51 @@
 # (CMakeLists.txt:46-62: no fast-math, default --fmad=true, device -O3), only with the
 # architecture set to sm_103a.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   stage and build everything from the reference tree
+#        oracle/build_ref.sh --staged         build libref_cpu.so from oracle/_ref/src only
 set -euo pipefail
-REF="${1:-/root/reference}"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
+SRC="$OUT/src"
+CUDA_HOME="${CUDA_HOME:-/usr/local/cuda}"
+NVCC="$CUDA_HOME/bin/nvcc"
+if [ $# -ne 1 ]; then
+  echo "usage: $0 REFERENCE_ROOT | --staged" >&2
+  exit 2
+fi
 mkdir -p "$OUT"
+
+build_cpu() {
+  # Reference CPU path.  -O2 stands in for a Release build (the CMake file sets no build type).
+  # -ffp-contract=off: the reference's x86-64 build has no FMA, so a*b+c is never contracted there;
+  # gcc on aarch64 would contract it by default and change the results.
+  g++ -O2 -fopenmp -std=c++17 -fPIC -shared -w -ffp-contract=off \
+      -I"$HERE/trimesh_shim" -I"$SRC" -I"$CUDA_HOME/include" \
+      "$HERE/ref_cpu_shim.cpp" "$SRC/cpu_voxelizer.cpp" \
+      -o "$OUT/libref_cpu.so"
+}
+
+if [ "$1" = "--staged" ]; then
+  if [ ! -f "$SRC/cpu_voxelizer.cpp" ]; then
+    echo "build_ref: no staged reference sources in $SRC; skipping" >&2
+    exit 0
+  fi
+  build_cpu
+  echo "build_ref: wrote libref_cpu.so from the staged sources"
+  exit 0
+fi
+
+REF="$1"
 if [ ! -f "$REF/src/cpu_voxelizer.cpp" ]; then
   echo "build_ref: reference sources not found under $REF; skipping" >&2
   exit 0
 fi
-CUDA_HOME="${CUDA_HOME:-/usr/local/cuda}"
-NVCC="$CUDA_HOME/bin/nvcc"
+mkdir -p "$SRC/libs/cuda"
+for f in cpu_voxelizer.cpp cpu_voxelizer.h util.h timer.h morton_LUTs.h libs/cuda/helper_math.h; do
+  cp "$REF/src/$f" "$SRC/$f"
+done
 
-# Reference CPU path.  -O2 stands in for a Release build (the CMake file sets no build type);
-# the x86-64 baseline has no FMA, so gcc cannot contract a*b+c here.
-g++ -O2 -fopenmp -std=c++17 -fPIC -shared -w \
-    -I"$HERE/trimesh_shim" -I"$REF/src" -I"$CUDA_HOME/include" \
-    "$HERE/ref_cpu_shim.cpp" "$REF/src/cpu_voxelizer.cpp" \
-    -o "$OUT/libref_cpu.so" &
+build_cpu &
 pid_cpu=$!
 
 # Reference output writers (src/util_io.cpp with its vendored MagicaVoxel writer), host code.

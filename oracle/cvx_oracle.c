@@ -55,9 +55,14 @@ typedef struct {
     int edge_xy;    /* per-voxel dot(n_xy,p_xy): 1 = fma(a.x,px,a.y*py), 2 = fma(a.y,py,a.x*px) */
     int edge_yz;    /* per-voxel dot(n_yz,p_yz): 1 = fma(a.x,py,a.y*pz), 2 = fma(a.y,pz,a.x*py) */
     int edge_zx;    /* per-voxel dot(n_zx,p_zx): 1 = fma(a.x,pz,a.y*px), 2 = fma(a.y,px,a.x*pz) */
-    int ccw;        /* solid checkCCW / check_point_triangle a*b-c*d: as cross */
+    int ccw;        /* solid checkCCW e0.x*e1.y - e1.x*e0.y: as cross */
+    int pt;         /* solid check_point_triangle t1..t3 a*b-c*d: as cross */
     int getx;       /* solid get_x_coordinate n.y*A+n.z*B: 1 = fma(n.y,A,n.z*B), 2 = fma(n.z,B,n.y*A)
                      * (the reference GPU kernel's linear-order code uses 1, its Morton-order code 2) */
+    int clip;       /* solid: keep the writes inside the grid the way the CUDA engine does where the
+                     * reference writes outside its table (columns outside the grid are dropped;
+                     * Morton order stops a run at x = gx; linear order continues a run into the
+                     * following rows up to the last voxel of the grid) */
     const float* inv_len; /* optional per-triangle rsqrtf(dot(c,c)) values from the device */
 } ovx_mode;
 
@@ -319,6 +324,8 @@ static void solid_triangle(const ovx_info* info, const float* tri, uint64_t t, u
                            uint64_t table_words, int morton, const ovx_mode* m) {
     const int gpu = m != NULL;
     const int pc = gpu ? m->cross : 0, p3 = gpu ? m->dot3 : 0, pw = gpu ? m->ccw : 0, pg = gpu ? m->getx : 0;
+    const int pp = gpu ? m->pt : 0, clip = gpu && m->clip;
+    const uint64_t total_bits = (uint64_t)info->grid[0] * info->grid[1] * info->grid[2];
     const f3 bmin = mk3(info->bmin[0], info->bmin[1], info->bmin[2]);
     const f3 unit = mk3(info->unit[0], info->unit[1], info->unit[2]);
     f3 v0 = sub3(mk3(tri[0], tri[1], tri[2]), bmin);
@@ -356,7 +363,8 @@ static void solid_triangle(const ovx_info* info, const float* tri, uint64_t t, u
             f2 point;
             if (gpu) point = mk2((float)(((double)y + 0.5) * (double)unit.y), (float)(((double)z + 0.5) * (double)unit.z));
             else point = mk2(((float)y + 0.5f) * unit.y, ((float)z + 0.5f) * unit.z);
-            int checknum = check_point_triangle(pw, v0_yz, v1_yz, v2_yz, point);
+            if (clip && (y < 0 || z < 0 || (uint32_t)y >= info->grid[1] || (uint32_t)z >= info->grid[2])) continue;
+            int checknum = check_point_triangle(pp, v0_yz, v1_yz, v2_yz, point);
             if ((checknum == 1 && top_left_edge(v0_yz, v1_yz)) || (checknum == 2 && top_left_edge(v1_yz, v2_yz)) ||
                 (checknum == 3 && top_left_edge(v2_yz, v0_yz)) || (checknum == 0)) {
                 int xmax = d2i((double)(get_x_coordinate(pg, n, v0, point) / unit.x) - 0.5);
@@ -368,8 +376,22 @@ static void solid_triangle(const ovx_info* info, const float* tri, uint64_t t, u
                     g_hits++;
                     continue;
                 }
+                if (clip && !morton && !g_parallel) {
+                    /* the same bits as the loop below (x = 0..xmax of the row, continuing into the
+                     * following rows, up to the grid's last voxel), XORed a word at a time */
+                    const uint64_t lo = (uint64_t)y * info->grid[0] + (uint64_t)z * ((uint64_t)info->grid[1] * info->grid[0]);
+                    if (lo >= total_bits) continue;
+                    const uint64_t hi = lo + (uint64_t)xmax < total_bits ? lo + (uint64_t)xmax : total_bits - 1;
+                    for (uint64_t w = lo / 32u; w <= hi / 32u; w++) {
+                        const uint32_t a = w == lo / 32u ? (uint32_t)(lo % 32u) : 0u;
+                        const uint32_t b = w == hi / 32u ? (uint32_t)(hi % 32u) : 31u;
+                        table[w] ^= (0xFFFFFFFFu >> a) & (0xFFFFFFFFu << (31u - b));
+                    }
+                    continue;
+                }
                 for (int64_t x = 0; x <= xmax; x++) {
                     uint64_t loc;
+                    if (clip && morton && (uint64_t)x >= info->grid[0]) break;
                     if (morton) {
                         loc = ovx_morton_encode((uint32_t)x, (uint32_t)y, (uint32_t)z);
                     } else if (gpu) {
@@ -377,6 +399,7 @@ static void solid_triangle(const ovx_info* info, const float* tri, uint64_t t, u
                     } else {
                         loc = (uint64_t)x + (uint64_t)(int64_t)y * info->grid[1] + (uint64_t)(int64_t)z * (uint64_t)info->grid[1] * (uint64_t)info->grid[2];
                     }
+                    if (clip && loc >= total_bits) break;
                     if (loc / 32u >= table_words) continue; /* the reference writes out of bounds here */
                     set_bit_xor(table, loc);
                 }
@@ -400,6 +423,24 @@ void ovx_voxelize(const ovx_info* info, const float* tris, uint32_t* table, int 
     for (uint64_t t = 0; t < info->n_tri; t++) {
         if (solid) solid_triangle(info, tris + 9 * t, t, table, words, morton, mode);
         else surface_triangle(info, tris + 9 * t, t, table, morton, mode);
+    }
+}
+
+/* dot(c, c) of each triangle's cross product c = cross(e0, e1) under mode m's patterns (the value
+ * the reference kernels pass to rsqrtf in normalize, helper_math.h:1436-1439), so that a caller can
+ * evaluate the device's rsqrtf on it and hand the results back as m->inv_len. */
+void ovx_len2(const ovx_info* info, const float* tris, const ovx_mode* m, float* out) {
+    const int pc = m ? m->cross : 0, p3 = m ? m->dot3 : 0;
+    const f3 bmin = mk3(info->bmin[0], info->bmin[1], info->bmin[2]);
+    for (uint64_t t = 0; t < info->n_tri; t++) {
+        const float* tri = tris + 9 * t;
+        f3 v0 = sub3(mk3(tri[0], tri[1], tri[2]), bmin);
+        f3 v1 = sub3(mk3(tri[3], tri[4], tri[5]), bmin);
+        f3 v2 = sub3(mk3(tri[6], tri[7], tri[8]), bmin);
+        f3 e0 = sub3(v1, v0), e1 = sub3(v2, v1);
+        f3 cr = mk3(mul_sub(pc, e0.y, e1.z, e0.z, e1.y), mul_sub(pc, e0.z, e1.x, e0.x, e1.z),
+                    mul_sub(pc, e0.x, e1.y, e0.y, e1.x));
+        out[t] = dot3p(p3, cr, cr);
     }
 }
 

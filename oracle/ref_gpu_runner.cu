@@ -118,4 +118,23 @@ int refgpu_voxelize(const void* info64, const float* d_tris, uint32_t* d_table, 
 
 int refgpu_block_size(int solid) { return solid ? g_solid.block : g_surface.block; }
 
+// out[i] = rsqrtf(in[i]) evaluated on the device: the 1/|n| factor of the reference kernels'
+// normalize() (helper_math.h:1436-1439), for the oracle's GPU-arithmetic mode (ovx_mode.inv_len).
+__global__ void rsqrt_kernel(const float* in, float* out, uint64_t n) {
+	const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) out[i] = rsqrtf(in[i]);
+}
+
+int refgpu_rsqrt(const float* d_in, float* d_out, uint64_t n, void* stream) {
+	if (n == 0) return 0;
+	const uint64_t blocks = (n + 255) / 256;
+	rsqrt_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(d_in, d_out, n);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) {
+		std::snprintf(g_err, sizeof(g_err), "rsqrt_kernel: %s", cudaGetErrorString(e));
+		return -1;
+	}
+	return 0;
+}
+
 }  // extern "C"

@@ -75,6 +75,18 @@ def test_morton_needs_cubic_power_of_two():
         assert _lib.lib.cvx_voxelize_solid(ctypes.byref(info), 1, 1, 1, None) == 2
 
 
+def test_noalloc_applies_the_per_axis_limit():
+    """cvx_voxelize_solid_noalloc refuses an axis above 2^22 like cvx_voxelize_solid, although a
+    2^23 x 2 x 1 grid fits its fixed scratch; the checks run before any CUDA call."""
+    info = _info()
+    info.gridsize[0], info.gridsize[1], info.gridsize[2] = 1 << 23, 2, 1
+    assert _lib.lib.cvx_voxelize_solid_noalloc(ctypes.byref(info), 1, 1, 0, None) == 2
+    assert b"above 2^22" in _lib.lib.cvx_last_error_message()
+    assert _lib.lib.cvx_voxelize_solid_noalloc(None, 1, 1, 0, None) == 1
+    m = cv.make_info((0, 0, 0), (1, 1, 1), (100, 100, 100), 1)
+    assert _lib.lib.cvx_voxelize_solid_noalloc(ctypes.byref(m), 1, 1, 1, None) == 2
+
+
 def test_empty_mesh_is_a_no_op():
     info = _info(n=0)
     assert _lib.lib.cvx_voxelize(ctypes.byref(info), None, 1, 0, None) == 0
