@@ -56,6 +56,9 @@ def parse(argv=None):
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["engine", "reference"], default="engine")
     p.add_argument("--no-extras", action="store_true", help="skip the soup / batch / serve side measurements")
+    p.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
+                   help="run one named workload 1 + --reps times for a profiler, then exit (no JSON line)")
+    p.add_argument("--reps", type=int, default=1, help="runs after the warm-up run of --profile-case")
     p.add_argument("--serve-seconds", type=float, default=2.0,
                    help="length of the open-loop serving runs at 25%% and 50%% load and of the plain arms")
     p.add_argument("--serve-long-seconds", type=float, default=60.0,
@@ -267,7 +270,7 @@ def step_roofline(cv, torch, T, table_bytes, hbm_gbs, ms_per_step):
         return None
     words = 32 << 20
     buf = torch.zeros(words, dtype=torch.int32, device="cuda")
-    r_atom = max(_lib.lib.cvx_microbench_atomic_or(buf.data_ptr(), words, 0, 152 * 8, 64) for _ in range(3))
+    r_atom = max(_lib.diag_lib().cvx_microbench_atomic_or(buf.data_ptr(), words, 0, 152 * 8, 64) for _ in range(3))
     del buf
     calls, sum_b, sum_a = {}, 0.0, 0.0
     for (morton, solid), name in zip(MODES, ("surface_linear", "surface_morton", "solid_linear", "solid_morton")):
@@ -374,8 +377,147 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ---- named workloads for kernel profiling (--profile-case) ---------------------------------------
+# Each builds its seeded synthetic input and returns a function that runs the engine once; main()
+# runs it 1 + --reps times, synchronising after each, so that a profiler can skip the warm-up
+# launches (ncu -s) and capture the ones after.
+
+def _pc_table(cv, torch, info):
+    return torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+
+
+def pc_ico8(cv, meshgen, torch):
+    """displaced icosphere, 8 subdivisions (1,310,720 triangles) at 512^3, four calls: surface
+    linear, surface Morton, solid linear, solid Morton"""
+    tris = meshgen.icosphere(0, level=8)
+    info = cv.make_voxinfo(tris, 512)
+    d = torch.from_numpy(tris.reshape(-1)).cuda()
+    tabs = [_pc_table(cv, torch, info) for _ in MODES]
+
+    def run():
+        for (morton, solid), tab in zip(MODES, tabs):
+            tab.zero_()
+            (cv.voxelize_solid if solid else cv.voxelize)(info, d, tab, morton)
+    return run
+
+
+def pc_ico8_plan(cv, meshgen, torch):
+    """the benchmark step: the same four jobs as one cvx_plan that clears its tables (clear_ranges)"""
+    tris = meshgen.icosphere(0, level=8)
+    info = cv.make_voxinfo(tris, 512)
+    d = torch.from_numpy(tris.reshape(-1)).cuda()
+    tabs = [_pc_table(cv, torch, info) for _ in MODES]
+    plan = cv.Plan([cv.Job(info, d, t, morton, solid) for (morton, solid), t in zip(MODES, tabs)], clear_tables=True)
+    return plan.launch
+
+
+def pc_soup(cv, meshgen, torch):
+    """2,000,000-triangle soup (edges log-uniform in [0.25, 512] voxels) at 1024^3, surface"""
+    tris = meshgen.soup(0, n=2_000_000)
+    info = cv.make_voxinfo(tris, 1024)
+    d = torch.from_numpy(tris.reshape(-1)).cuda()
+    tab = _pc_table(cv, torch, info)
+
+    def run():
+        tab.zero_()
+        cv.voxelize(info, d, tab)
+    return run
+
+
+def pc_soup200k(cv, meshgen, torch):
+    """the first 200,000 triangles of that soup at 1024^3 (a small case of the brick kernels)"""
+    tris = meshgen.soup(0, n=2_000_000)[:200_000]
+    info = cv.make_voxinfo(tris, 1024)
+    d = torch.from_numpy(tris.reshape(-1)).cuda()
+    tab = _pc_table(cv, torch, info)
+
+    def run():
+        tab.zero_()
+        cv.voxelize(info, d, tab)
+    return run
+
+
+def pc_soup200k_rows(cv, meshgen, torch):
+    """the same with the brick rasterizer off (brick_pairs = 0): every larger triangle row by row"""
+    cv.set_tuning(torch.cuda.current_device(), brick_pairs=0)
+    return pc_soup200k(cv, meshgen, torch)
+
+
+def _pc_mix_jobs(cv, meshgen, torch, select):
+    jobs = []
+    for spec in meshgen.batch_mix(0, 256):
+        if not select(spec):
+            continue
+        t = spec.build()
+        info = cv.make_voxinfo(t, spec.gridsize)
+        jobs.append(cv.Job(info, torch.from_numpy(t.reshape(-1)).cuda(), _pc_table(cv, torch, info), spec.morton,
+                           spec.solid))
+    return jobs
+
+
+def pc_batch(cv, meshgen, torch):
+    """the 256-mesh uneven mix (triangle counts 1k-500k, grids 64-512, 3:1 surface:solid, 1:1
+    linear:Morton) as one cvx_voxelize_batch"""
+    jobs = _pc_mix_jobs(cv, meshgen, torch, lambda spec: True)
+
+    def run():
+        for j in jobs:
+            j.table.zero_()
+        cv.voxelize_batch(jobs)
+    return run
+
+
+def pc_batch_g512(cv, meshgen, torch):
+    """the surface meshes of that mix gridded at 512^3, as one batch"""
+    jobs = _pc_mix_jobs(cv, meshgen, torch, lambda spec: not spec.solid and spec.gridsize == 512)
+
+    def run():
+        for j in jobs:
+            j.table.zero_()
+        cv.voxelize_batch(jobs)
+    return run
+
+
+def pc_io(cv, meshgen, torch):
+    """a random 1024^3 table transcoded linear -> Morton -> linear, then the 512^3 solid icosphere's
+    binvox payload and voxel list"""
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    tab = torch.randint(-2 ** 31, 2 ** 31 - 1, (1024 ** 3 // 32,), dtype=torch.int32, device="cuda", generator=gen)
+    tris = meshgen.icosphere(0, level=8)
+    info = cv.make_voxinfo(tris, 512)
+    t512 = _pc_table(cv, torch, info)
+    cv.voxelize_solid(info, torch.from_numpy(tris.reshape(-1)).cuda(), t512)
+
+    def run():
+        m = cv.transcode(tab, 1024, True)
+        cv.transcode(m, 1024, False)
+        cv.encode_binvox(info, t512)
+        cv.encode_voxel_list(info, t512)
+    return run
+
+
+PROFILE_CASES = {"ico8": pc_ico8, "ico8_plan": pc_ico8_plan, "soup": pc_soup, "soup200k": pc_soup200k,
+                 "soup200k_rows": pc_soup200k_rows,
+                 "batch": pc_batch, "batch_g512": pc_batch_g512, "io": pc_io}
+
+
+def run_profile_case(name, reps):
+    import torch
+    import cuda_voxelizer_gb300 as cv
+    from cuda_voxelizer_gb300 import meshgen
+    run = PROFILE_CASES[name](cv, meshgen, torch)
+    for _ in range(1 + reps):
+        run()
+        torch.cuda.synchronize()
+    cv.device_status()
+    print(f"{name}: {1 + reps} runs done")
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        run_profile_case(args.profile_case, args.reps)
+        return
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
@@ -387,6 +529,14 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
+    # The autotuner's choice of the tuning knobs for this device (results never depend on them),
+    # timed once here and cached; every number below runs with it.
+    from cuda_voxelizer_gb300 import autotune
+    default_tuning = cv.get_tuning(local)
+    tuned = autotune.autotune(local, reps=3)
+    tuning = {"choice": {k: tuned[k] for k in autotune.KNOBS}, "default": default_tuning,
+              "tuning_set_ms": {"tuned": tuned["ms"], "default": tuned["default_ms"]},
+              "seconds": tuned["seconds"]}
     tris = meshgen.icosphere(0, level=8)
     info = cv.make_voxinfo(tris, 512)
     T = tris.shape[0]
@@ -572,7 +722,7 @@ def main():
             "config": {"workload": "icosphere level 8 (1,310,720 tris) at 512^3; surface+solid x linear+Morton "
                                    "per step", "gridsize": 512, "triangles": T, "l2": "flushed between steps "
                                    "(512 MiB write, untimed)", "parallelism": f"replicas x{world}"},
-            "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps, "e2e": e2e,
+            "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps, "e2e": e2e, "tuning": tuning,
             "roofline": roofline, "step_per_call": step_calls, "step_sequential": step_seq_line}
 
     if rank == 0:
@@ -589,7 +739,7 @@ def main():
             specs = meshgen.batch_mix(0, 256)
             mix = [(s, s.build()) for s in specs]
             extras.update(bench_io(cv, meshgen, torch, flush))
-            extras.update(bench_batch(cv, torch, mix))
+            extras.update(bench_batch(cv, torch, mix, default_tuning))
             extras.update(bench_serve(cv, meshgen, torch, mix, args.serve_seconds, args.serve_long_seconds,
                                       extras["batch_256"]["plan_meshes_s"]))
         line["extras"] = extras
@@ -631,7 +781,7 @@ def bench_soup(cv, meshgen, torch, stream, flush):
             a = int(json.load(f)["soup_2m_1024"]["surface_linear"])
         words = 32 << 20
         buf = torch.zeros(words, dtype=torch.int32, device="cuda")
-        r_atom = max(_lib.lib.cvx_microbench_atomic_or(buf.data_ptr(), words, 0, 152 * 8, 64) for _ in range(3))
+        r_atom = max(_lib.diag_lib().cvx_microbench_atomic_or(buf.data_ptr(), words, 0, 152 * 8, 64) for _ in range(3))
         del buf
         b = 36 * 2_000_000 + 4 * cv.table_words(info)
         hbm, _ = peaks()
@@ -729,24 +879,37 @@ def bench_io(cv, meshgen, torch, flush):
     return {"io": out}
 
 
-def bench_batch(cv, torch, mix):
-    """256-mesh uneven mix: one graph launch (plan) vs plain per-mesh synchronous calls."""
+def bench_batch(cv, torch, mix, default_tuning=None):
+    """256-mesh uneven mix: one graph launch (plan) vs plain per-mesh synchronous calls, with the
+    autotuner's choice in effect; the plan is also timed with the default tuning."""
     jobs = []
     for s, t in mix:
         info = cv.make_voxinfo(t, s.gridsize)
         jobs.append(cv.Job(info, torch.from_numpy(t.reshape(-1)).cuda(),
                            torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda"), s.morton, s.solid))
     n_tris = sum(int(j.info.n_triangles) for j in jobs)
-    plan = cv.Plan(jobs, clear_tables=True)
-    for _ in range(3):
-        plan.launch()
-    torch.cuda.synchronize()
     reps = 5
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        plan.launch()
-    torch.cuda.synchronize()
-    plan_s = (time.perf_counter() - t0) / reps
+
+    def time_plan():
+        plan = cv.Plan(jobs, clear_tables=True)
+        for _ in range(3):
+            plan.launch()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            plan.launch()
+        torch.cuda.synchronize()
+        plan.close()
+        return (time.perf_counter() - t0) / reps
+
+    default_plan_ms = None
+    if default_tuning:
+        tuned = cv.get_tuning(torch.cuda.current_device())
+        cv.set_tuning(torch.cuda.current_device(), **default_tuning)
+        default_plan_ms = time_plan() * 1e3
+        cv.set_tuning(torch.cuda.current_device(), **tuned)
+    plan_s = time_plan()
+    plan = cv.Plan(jobs, clear_tables=True)
     # plain: what a caller of the reference drop-in does, one synchronous call per mesh
     def plain():
         for j in jobs:
@@ -761,7 +924,7 @@ def bench_batch(cv, torch, mix):
     plan.close()
     return {"batch_256": {"meshes": 256, "triangles": n_tris, "plan_ms": plan_s * 1e3, "plain_ms": plain_s * 1e3,
                           "plan_meshes_s": 256 / plan_s, "plain_meshes_s": 256 / plain_s,
-                          "speedup_vs_plain": plain_s / plan_s}}
+                          "speedup_vs_plain": plain_s / plan_s, "plan_ms_default_tuning": default_plan_ms}}
 
 
 def copy_rates(torch, nbytes=1 << 30):

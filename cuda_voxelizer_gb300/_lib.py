@@ -57,7 +57,7 @@ class CvxServerStats(ctypes.Structure):
 
 
 class CvxTuning(ctypes.Structure):
-    _fields_ = [("small_vox", ctypes.c_uint32), ("small_cols", ctypes.c_uint32)]
+    _fields_ = [("small_vox", ctypes.c_uint32), ("small_cols", ctypes.c_uint32), ("brick_pairs", ctypes.c_uint32)]
 
 
 assert ctypes.sizeof(CvxVoxinfo) == 64
@@ -102,7 +102,6 @@ SIGNATURES = {
     "cvx_set_tuning": (c_status, [ctypes.c_int, ctypes.POINTER(CvxTuning)]),
     "cvx_profile_enable": (c_status, [ctypes.c_int]),
     "cvx_profile_collect": (ctypes.c_int, [ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
-    "cvx_microbench_atomic_or": (ctypes.c_double, [vp, u64, ctypes.c_int, u32, u32]),
 }
 
 for _name, (_res, _args) in SIGNATURES.items():
@@ -124,3 +123,18 @@ class CvxError(RuntimeError):
 def check(status: int, where: str) -> None:
     if status != 0:
         raise CvxError(status, where)
+
+
+def diag_lib():
+    """libcvx_diag.so (include/cvx_diag.h): the atomicOr-rate measurement behind the roofline.  Not
+    part of the voxelization library; loaded on demand by measurement code."""
+    global _diag
+    try:
+        return _diag
+    except NameError:
+        pass
+    d = ctypes.CDLL(os.path.join(_HERE, "_lib", "libcvx_diag.so"))
+    d.cvx_microbench_atomic_or.restype = ctypes.c_double
+    d.cvx_microbench_atomic_or.argtypes = [vp, u64, ctypes.c_int, u32, u32]
+    _diag = d
+    return d

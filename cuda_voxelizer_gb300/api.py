@@ -170,12 +170,21 @@ def voxelize_batch(jobs: Sequence[Job], stream=None) -> None:
     check(lib.cvx_voxelize_batch(arr, len(jobs), _stream(stream)), "cvx_voxelize_batch")
 
 
+def _apply_tuning() -> None:
+    """The device's cached autotuner choice (cuda_voxelizer_gb300.autotune), applied once per device
+    and process before the first plan or server is built; without a cache the defaults stay."""
+    import torch
+    from . import autotune
+    autotune.apply_cached_once(torch.cuda.current_device())
+
+
 class Plan:
     """A batch captured once into a CUDA graph and replayed with one launch."""
 
     CLEAR_TABLES = 1
 
     def __init__(self, jobs: Sequence[Job], clear_tables: bool = True):
+        _apply_tuning()
         self._jobs = list(jobs)  # keep buffers alive
         arr = _jobs_array(self._jobs)
         h = ctypes.c_void_p()
@@ -268,13 +277,15 @@ def profile_collect(max_entries: int = 4096) -> list:
 def get_tuning(device: int = 0) -> dict:
     t = CvxTuning()
     check(lib.cvx_get_tuning(device, ctypes.byref(t)), "cvx_get_tuning")
-    return {"small_vox": t.small_vox, "small_cols": t.small_cols}
+    return {"small_vox": t.small_vox, "small_cols": t.small_cols, "brick_pairs": t.brick_pairs}
 
 
-def set_tuning(device: int = 0, small_vox: int | None = None, small_cols: int | None = None) -> None:
+def set_tuning(device: int = 0, small_vox: int | None = None, small_cols: int | None = None,
+               brick_pairs: int | None = None) -> None:
     cur = get_tuning(device)
     t = CvxTuning(small_vox if small_vox is not None else cur["small_vox"],
-                  small_cols if small_cols is not None else cur["small_cols"])
+                  small_cols if small_cols is not None else cur["small_cols"],
+                  brick_pairs if brick_pairs is not None else cur["brick_pairs"])
     check(lib.cvx_set_tuning(device, ctypes.byref(t)), "cvx_set_tuning")
 
 
@@ -313,6 +324,7 @@ class Server:
     the request has been waited for."""
 
     def __init__(self, memory_budget_bytes: int = 40 << 30, max_batch: int = 256, max_inflight: int = 4):
+        _apply_tuning()
         cfg = CvxServerConfig(int(memory_budget_bytes), int(max_batch), int(max_inflight))
         h = ctypes.c_void_p()
         check(lib.cvx_server_create(ctypes.byref(cfg), ctypes.byref(h)), "cvx_server_create")

@@ -1,13 +1,16 @@
-"""Autotuner for the engine's bin thresholds (cvx_tuning), with a per-device cache.
+"""Autotuner for the engine's tuning knobs (cvx_tuning), with a per-device cache.
 
-The thresholds decide which triangles a classify kernel finishes inside its CTA and which it
-queues for the cooperative kernels: ``small_vox`` (surface: triangles whose grid bounding box
-holds at most this many voxels are tested voxel by voxel in the classify kernel) and
-``small_cols`` (solid: triangles with at most this many voxel-centre columns).  Results never
-depend on them; only the time does.  ``autotune()`` times a fixed set of seeded workloads (sub-voxel
-and few-voxel triangles at several grids, surface and solid, linear and Morton) for every candidate
-pair, keeps the fastest, applies it with cvx_set_tuning and stores it in a JSON cache keyed by the
-device name; ``load_cached()`` applies a cached choice without timing anything.
+The knobs decide where a triangle's work goes; results never depend on them, only the time does:
+``small_vox`` (surface: triangles whose grid bounding box holds at most this many voxels are tested
+voxel by voxel in the classify kernel), ``small_cols`` (solid: triangles with at most this many
+voxel-centre columns stay in the classify kernel) and ``brick_pairs`` (surface, grids of 2^24+
+voxels: (brick, triangle) pairs per triangle the shared-memory brick rasterizer may use; 0 sends
+every larger triangle to the row-by-row path with global atomics).  ``autotune()`` times a fixed set
+of seeded workloads -- sub-voxel and few-voxel triangles at several grids, surface and solid, linear
+and Morton, and a soup of large triangles at 1024^3 -- for every candidate, keeps the fastest,
+applies it with cvx_set_tuning and stores it in a JSON cache keyed by the device; ``load_cached()``
+applies a cached choice without timing anything.  The package applies the cache once per device
+the first time a Plan or Server is made (``apply_cached_once``).
 
     python -m cuda_voxelizer_gb300.autotune            # tune device 0, print and cache the result
 """
@@ -24,7 +27,10 @@ from . import meshgen
 
 SMALL_VOX = (16, 32, 64, 128, 255)
 SMALL_COLS = (4, 8, 16)
-DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "cuda_voxelizer_gb300", "tuning.json")
+BRICK_PAIRS = (0, 8)
+KNOBS = ("small_vox", "small_cols", "brick_pairs")
+DEFAULT_CACHE = os.environ.get("CVX_TUNING_CACHE") or os.path.join(os.path.expanduser("~"), ".cache",
+                                                                     "cuda_voxelizer_gb300", "tuning.json")
 
 
 def _device_key(device: int) -> str:
@@ -45,6 +51,9 @@ def _workloads(torch):
             for morton in (False, True):
                 out.append((f"{name}_{'solid' if solid else 'surf'}_{'mor' if morton else 'lin'}", info, d, solid,
                             morton))
+    soup = meshgen.soup(14, n=200_000)
+    out.append(("soup200k_g1024_surf_lin", cv.make_voxinfo(soup, 1024), torch.from_numpy(soup.reshape(-1)).cuda(),
+                False, False))
     return out
 
 
@@ -69,8 +78,22 @@ def _time_all(torch, work, tables, reps):
     return total
 
 
+def _write_cache(cache_path: str, key: str, choice: dict) -> None:
+    cache = {}
+    if os.path.exists(cache_path):
+        try:
+            with open(cache_path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    cache[key] = choice
+    os.makedirs(os.path.dirname(cache_path), exist_ok=True)
+    with open(cache_path, "w") as f:
+        json.dump(cache, f, indent=1)
+
+
 def autotune(device: int = 0, cache_path: str | None = DEFAULT_CACHE, reps: int = 5, verbose: bool = False) -> dict:
-    """Times every (small_vox, small_cols) candidate, applies and caches the fastest."""
+    """Times every (small_vox, small_cols, brick_pairs) candidate, applies and caches the fastest."""
     import torch
     torch.cuda.set_device(device)
     work = _workloads(torch)
@@ -80,34 +103,26 @@ def autotune(device: int = 0, cache_path: str | None = DEFAULT_CACHE, reps: int 
     t0 = time.perf_counter()
     for sv in SMALL_VOX:
         for sc in SMALL_COLS:
-            cv.set_tuning(device, small_vox=sv, small_cols=sc)
-            ms = _time_all(torch, work, tables, reps)
-            results.append({"small_vox": sv, "small_cols": sc, "ms": ms})
-            if verbose:
-                print(f"small_vox={sv:3d} small_cols={sc:2d}: {ms:.3f} ms", flush=True)
+            for bp in BRICK_PAIRS:
+                cv.set_tuning(device, small_vox=sv, small_cols=sc, brick_pairs=bp)
+                ms = _time_all(torch, work, tables, reps)
+                results.append({"small_vox": sv, "small_cols": sc, "brick_pairs": bp, "ms": ms})
+                if verbose:
+                    print(f"small_vox={sv:3d} small_cols={sc:2d} brick_pairs={bp}: {ms:.3f} ms", flush=True)
     best = min(results, key=lambda r: r["ms"])
-    cv.set_tuning(device, small_vox=best["small_vox"], small_cols=best["small_cols"])
-    out = {"device": _device_key(device), "small_vox": best["small_vox"], "small_cols": best["small_cols"],
-           "ms": best["ms"], "default": before, "default_ms": next(
-               (r["ms"] for r in results if r["small_vox"] == before["small_vox"] and r["small_cols"] ==
-                before["small_cols"]), None), "candidates": results, "seconds": time.perf_counter() - t0}
+    choice = {k: best[k] for k in KNOBS}
+    cv.set_tuning(device, **choice)
+    out = {"device": _device_key(device), **choice, "ms": best["ms"], "default": before,
+           "default_ms": next((r["ms"] for r in results if all(r[k] == before[k] for k in KNOBS)), None),
+           "candidates": results, "seconds": time.perf_counter() - t0}
     if cache_path:
-        cache = {}
-        if os.path.exists(cache_path):
-            try:
-                with open(cache_path) as f:
-                    cache = json.load(f)
-            except (OSError, ValueError):
-                cache = {}
-        cache[out["device"]] = {"small_vox": out["small_vox"], "small_cols": out["small_cols"]}
-        os.makedirs(os.path.dirname(cache_path), exist_ok=True)
-        with open(cache_path, "w") as f:
-            json.dump(cache, f, indent=1)
+        _write_cache(cache_path, out["device"], choice)
     return out
 
 
 def load_cached(device: int = 0, cache_path: str = DEFAULT_CACHE) -> dict | None:
-    """Applies this device's cached thresholds, if any; returns them (None when not cached)."""
+    """Applies this device's cached choice, if any; returns it (None when not cached).  Knobs the
+    cache does not name keep their current values."""
     try:
         with open(cache_path) as f:
             entry = json.load(f).get(_device_key(device))
@@ -115,8 +130,20 @@ def load_cached(device: int = 0, cache_path: str = DEFAULT_CACHE) -> dict | None
         return None
     if not entry:
         return None
-    cv.set_tuning(device, small_vox=int(entry["small_vox"]), small_cols=int(entry["small_cols"]))
-    return entry
+    choice = {k: int(entry[k]) for k in KNOBS if k in entry}
+    cv.set_tuning(device, **choice)
+    return choice
+
+
+_applied: set = set()
+
+
+def apply_cached_once(device: int = 0) -> dict | None:
+    """load_cached(device) the first time it is called for `device` in this process."""
+    if device in _applied:
+        return None
+    _applied.add(device)
+    return load_cached(device)
 
 
 if __name__ == "__main__":

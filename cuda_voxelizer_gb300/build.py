@@ -17,7 +17,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libcvx.so")
-SOURCES = ["surface.cu", "solid.cu", "api.cu", "dropin.cpp", "microbench.cu", "noalloc.cu", "server.cu", "clear.cu", "mesh.cu", "transcode.cu", "encode.cu"]
+DIAG_LIB = os.path.join(OUT_DIR, "libcvx_diag.so")  # include/cvx_diag.h: measurement helpers, not the ABI
+DIAG_SOURCES = ["microbench.cu"]
+SOURCES = ["surface.cu", "bricks.cu", "solid.cu", "api.cu", "dropin.cpp", "noalloc.cu", "server.cu", "clear.cu", "mesh.cu", "transcode.cu", "encode.cu"]
 HEADERS = ["cvx_device.cuh", "surface.cuh", "engine.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -68,13 +70,13 @@ def build(verbose: bool = False, extra_flags=None) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     nvcc = nvcc_path()
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", h)
-                                                         for h in ("cvx.h", "cvx_dropin.h")]
-    objs = []
+                                                         for h in ("cvx.h", "cvx_dropin.h", "cvx_diag.h")]
+    objs, diag_objs = [], []
     jobs = []
-    for src in SOURCES:
+    for src in SOURCES + DIAG_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT_DIR, src + ".o")
-        objs.append(o)
+        (diag_objs if src in DIAG_SOURCES else objs).append(o)
         if _stale(o, [s, __file__] + hdrs):
             cmd = [nvcc] + _flags() + list(extra_flags or []) + ["-c", s, "-o", o]
             jobs.append(cmd)
@@ -87,14 +89,14 @@ def build(verbose: bool = False, extra_flags=None) -> str:
             raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
         return r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + len(DIAG_SOURCES)) as ex:
         for err in ex.map(run, jobs):
             if verbose and err:
                 print(err, file=sys.stderr)
-    if jobs or _stale(LIB, objs):
-        cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-o", LIB] + objs + \
-              ["-Xlinker", "-rpath," + cuda_lib_dir()]
-        run(cmd)
+    for lib, o in ((LIB, objs), (DIAG_LIB, diag_objs)):
+        if jobs or _stale(lib, o):
+            run([nvcc] + ARCH + ["-shared", "-cudart", "shared", "-Xlinker", "--no-undefined", "-o", lib] + o +
+                ["-Xlinker", "-rpath," + cuda_lib_dir()])
     return LIB
 
 

@@ -60,6 +60,7 @@ struct DevState {
 	int sms = 0;
 	int rows_grid = 0;
 	int cols_grid = 0;
+	int raster_grid = 0;
 	Tune tune;
 };
 
@@ -76,6 +77,7 @@ cvx_status dev_state(DevState& out, int* dev_out = nullptr) {
 		CVX_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
 		d.rows_grid = d.sms * surf_rows_blocks_per_sm();
 		d.cols_grid = d.sms * solid_cols_blocks_per_sm();
+		d.raster_grid = d.sms * brick_raster_blocks_per_sm();
 		it = g_dev.emplace(dev, d).first;
 	}
 	out = it->second;
@@ -103,17 +105,52 @@ const Prof* prof() { return g_profile ? &g_prof : nullptr; }
 
 // ---- scratch ------------------------------------------------------------------------------------
 
+// Record area of a launch sequence: counters, per-brick pair counts (for up to `bricks` bricks per
+// launch; none without JOB_BRICKS jobs), the queues (cap triangles), the other brick arrays, then
+// `n_jobs` uploaded job descriptors.  [0, big) must be zero before the first launch sequence on the
+// area (the counts are zero again after every sequence).  Pairs: about 27 per queued triangle on the
+// 1024^3 stress soup; triangles whose pairs do not fit are rasterized by surf_rows instead.
 struct RecLayout {
-	size_t ctr, big, mid, jobs, end;
+	size_t ctr, bcnt, big, mid, bq, tri, boff, bcur, ubeg, psorted, jobs, end;
+	uint64_t pair_cap;
 };
-RecLayout rec_layout(uint64_t cap, uint64_t n_jobs) {
+RecLayout rec_layout(uint64_t cap, uint64_t n_jobs, uint32_t bricks = 0) {
 	RecLayout l;
 	l.ctr = 0;
-	l.big = align_up(sizeof(Counters));
+	l.bcnt = align_up(sizeof(Counters));
+	l.big = align_up(l.bcnt + (uint64_t)bricks * 4);
 	l.mid = align_up(l.big + cap * sizeof(BigRec));
-	l.jobs = align_up(l.mid + cap * sizeof(MidRec));
+	l.bq = align_up(l.mid + cap * sizeof(MidRec));
+	l.pair_cap = bricks ? std::min<uint64_t>(std::max<uint64_t>(kMaxBrickPairs * cap, 1u << 16), 1ull << 31) : 0;
+	const uint64_t nq = bricks ? cap : 0;
+	l.tri = align_up(l.bq + nq * sizeof(MidRec));
+	l.boff = align_up(l.tri + nq * sizeof(BrickTri));
+	l.bcur = align_up(l.boff + (bricks ? (uint64_t)bricks + 1 : 0) * 4);
+	l.ubeg = align_up(l.bcur + (uint64_t)bricks * 4);
+	l.psorted = align_up(l.ubeg + (bricks ? (uint64_t)bricks + 1 : 0) * 4);
+	l.jobs = align_up(l.psorted + l.pair_cap * 4);
 	l.end = align_up(l.jobs + n_jobs * sizeof(JobDesc));
 	return l;
+}
+
+// Point a launch descriptor's scratch at a record area laid out by rec_layout(cap, *, bricks); the
+// tuning may use less of the pair area (brick_pairs per triangle; 0 sends every triangle to surf_rows).
+void bind_scratch(LaunchDesc& L, char* rec, uint64_t cap, uint32_t bricks, const Tune& tune) {
+	const RecLayout l = rec_layout(cap, 0, bricks);
+	L.scr.ctr = reinterpret_cast<Counters*>(rec + l.ctr);
+	L.scr.big = reinterpret_cast<BigRec*>(rec + l.big);
+	L.scr.mid = reinterpret_cast<MidRec*>(rec + l.mid);
+	L.scr.cap = (uint32_t)cap;
+	const uint64_t want = (uint64_t)std::min(tune.brick_pairs, kMaxBrickPairs) * cap;
+	L.scr.pair_cap = tune.brick_pairs ? (uint32_t)std::min<uint64_t>(std::max<uint64_t>(want, 1u << 16), l.pair_cap) : 0u;
+	if (!bricks) return;
+	L.scr.bq = reinterpret_cast<MidRec*>(rec + l.bq);
+	L.scr.tri = reinterpret_cast<BrickTri*>(rec + l.tri);
+	L.scr.brick_cnt = reinterpret_cast<uint32_t*>(rec + l.bcnt);
+	L.scr.brick_off = reinterpret_cast<uint32_t*>(rec + l.boff);
+	L.scr.brick_cur = reinterpret_cast<uint32_t*>(rec + l.bcur);
+	L.scr.unit_begin = reinterpret_cast<uint32_t*>(rec + l.ubeg);
+	L.scr.pair_sorted = reinterpret_cast<uint32_t*>(rec + l.psorted);
 }
 
 struct StreamScratch {
@@ -223,6 +260,7 @@ JobDesc make_job(const cvx_voxinfo& v, const float* tris, uint32_t* table, int m
 	j.flags = (morton ? JOB_MORTON : 0u) | (solid ? JOB_SOLID : 0u);
 	const uint64_t voxels = (uint64_t)v.gridsize[0] * v.gridsize[1] * v.gridsize[2];
 	if (morton ? v.gridsize[0] <= 1024 : voxels <= (1ull << 32)) j.flags |= JOB_NARROW;
+	if (!solid && brick_grid(j.grid)) j.flags |= JOB_BRICKS;
 	if (v.n_triangles && needs_plain_loads(tris)) j.flags |= JOB_PLAIN_LOADS;
 	return j;
 }
@@ -236,10 +274,11 @@ struct Group {
 	uint32_t tiles = 0, units = 0;
 	uint64_t mwords = 0, mbricks = 0, mslabs = 0;
 	uint32_t slab_smem = 0;
+	uint32_t bricks = 0;  // 64^3 bricks of the group's JOB_BRICKS jobs
 };
 
 void finish_group(Group& g, bool solid) {
-	uint32_t tile = 0, unit = 0;
+	uint32_t tile = 0, unit = 0, brick = 0;
 	uint64_t mw = 0, mb = 0, ms = 0;
 	g.tris = 0;
 	g.slab_smem = 0;
@@ -247,6 +286,8 @@ void finish_group(Group& g, bool solid) {
 		j.tile_begin = tile;
 		tile += tiles_of(j.n_tri);
 		g.tris += j.n_tri;
+		j.brick_begin = brick;  // running count: jobs without bricks take the next job's value
+		if (!solid && (j.flags & JOB_BRICKS)) brick += bricks_of(j.grid);
 		if (solid) {
 			j.unit_begin = unit;
 			// Morton slab grids are resolved by solid_morton_slab alone: no resolve units
@@ -272,6 +313,7 @@ void finish_group(Group& g, bool solid) {
 	}
 	g.tiles = tile;
 	g.units = unit;
+	g.bricks = brick;
 	g.mwords = mw;
 	g.mbricks = mb;
 	g.mslabs = ms;
@@ -333,6 +375,7 @@ struct Runner {
 	size_t jobs_used = 0;  // JobDesc slots used in the device job area
 	uint64_t cap;          // queue capacity (triangles)
 	size_t jobs_off;
+	uint32_t bricks = 0;   // brick capacity of the record area (largest group's bricks)
 	bool timed = true;     // per-kernel events for cvx_profile_collect (callers on this thread only)
 	const Prof* p() const { return timed ? prof() : nullptr; }
 
@@ -345,11 +388,9 @@ struct Runner {
 		L.n_mbricks = g.mbricks;
 		L.n_mslabs = g.mslabs;
 		L.slab_smem = g.slab_smem;
-		L.scr.ctr = reinterpret_cast<Counters*>(rec);
-		const RecLayout lay = rec_layout(cap, 0);
-		L.scr.big = reinterpret_cast<BigRec*>(rec + lay.big);
-		L.scr.mid = reinterpret_cast<MidRec*>(rec + lay.mid);
-		L.scr.cap = (uint32_t)cap;
+		if (g.bricks > bricks) return fail(CVX_ERR_INVALID_VALUE, "brick scratch too small");
+		L.n_bricks = g.bricks;
+		bind_scratch(L, rec, cap, bricks, dev.tune);
 		if (g.jobs.size() == 1) {
 			L.single = g.jobs[0];
 			L.jobs = nullptr;
@@ -372,7 +413,7 @@ struct Runner {
 			cvx_status st = prepare(g, L);
 			if (st != CVX_OK) return st;
 			CVX_CUDA(cudaMemsetAsync(rec, 0, kCountersResetBytes, s));
-			CVX_CUDA(launch_surface(L, dev.tune, dev.rows_grid, s, p()));
+			CVX_CUDA(launch_surface(L, dev.tune, dev.rows_grid, dev.raster_grid, s, p()));
 		}
 		if (!solid.empty()) {
 			for (Group& g : make_groups(solid, true)) {
@@ -403,6 +444,13 @@ size_t job_slots(const std::vector<JobDesc>& surf, const std::vector<JobDesc>& s
 	return n;
 }
 
+// Largest brick count of a surface launch group.
+uint32_t max_bricks(const std::vector<JobDesc>& surf) {
+	uint32_t m = 0;
+	for (const Group& g : make_groups(surf, false)) m = std::max(m, g.bricks);
+	return m;
+}
+
 uint64_t queue_cap(const std::vector<JobDesc>& a, const std::vector<JobDesc>& b) {
 	uint64_t m = 1;
 	for (const Group& g : make_groups(a, false)) m = std::max(m, g.tris);
@@ -430,7 +478,8 @@ cvx_status run_internal(std::vector<JobDesc> surf, std::vector<JobDesc> solid, c
 	for (const JobDesc& j : solid) flip_total += flip_bytes_of(j);
 	const uint64_t cap = queue_cap(surf, solid);
 	const size_t slots = job_slots(surf, solid);
-	const RecLayout lay = rec_layout(cap, slots);
+	const uint32_t bricks = max_bricks(surf);
+	const RecLayout lay = rec_layout(cap, slots, bricks);
 	StreamScratch* w = nullptr;
 	st = ensure_scratch(devid, s, lay.end, (size_t)flip_total, slots, &w);
 	if (st != CVX_OK) return st;
@@ -439,7 +488,8 @@ cvx_status run_internal(std::vector<JobDesc> surf, std::vector<JobDesc> solid, c
 	Runner r{s, dev, reinterpret_cast<char*>(w->rec), w->rec_bytes, w->flips, w->staging, w->staging_n};
 	r.cap = cap;
 	r.jobs_off = lay.jobs;
-	CVX_CUDA(cudaMemsetAsync(w->rec, 0, sizeof(Counters), s));
+	r.bricks = bricks;
+	CVX_CUDA(cudaMemsetAsync(w->rec, 0, lay.big, s));  // counters and brick counts
 	st = r.run(surf, solid);
 	if (st != CVX_OK) return st;
 	if (slots) CVX_CUDA(cudaEventRecord(w->staging_done, s));
@@ -472,7 +522,7 @@ cvx_status cvx::batch_scratch_bytes(const cvx_job* jobs, uint32_t n_jobs, size_t
 	cvx_status st = collect_jobs(jobs, n_jobs, nullptr, surf, solid);
 	if (st != CVX_OK) return st;
 	const size_t slots = job_slots(surf, solid);
-	*rec_bytes = rec_layout(queue_cap(surf, solid), slots).end;
+	*rec_bytes = rec_layout(queue_cap(surf, solid), slots, max_bricks(surf)).end;
 	*staging_bytes = std::max<size_t>(slots, 1) * sizeof(JobDesc);
 	return CVX_OK;
 }
@@ -489,7 +539,8 @@ cvx_status cvx::run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* con
 	if (!solid.empty() && !flips) return fail(CVX_ERR_INVALID_VALUE, "solid jobs need flip tables");
 	const uint64_t cap = queue_cap(surf, solid);
 	const size_t slots = job_slots(surf, solid);
-	const RecLayout lay = rec_layout(cap, slots);
+	const uint32_t bricks = max_bricks(surf);
+	const RecLayout lay = rec_layout(cap, slots, bricks);
 	if (!d_rec || rec_bytes < lay.end || reinterpret_cast<uintptr_t>(d_rec) % kAlign)
 		return fail(CVX_ERR_INVALID_VALUE, "record area too small or not 256-byte aligned");
 	if (slots && (!h_staging || staging_bytes < slots * sizeof(JobDesc)))
@@ -501,8 +552,9 @@ cvx_status cvx::run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* con
 	         staging_bytes / sizeof(JobDesc)};
 	r.cap = cap;
 	r.jobs_off = lay.jobs;
+	r.bricks = bricks;
 	r.timed = false;  // the server's worker thread: nobody collects events there
-	CVX_CUDA(cudaMemsetAsync(d_rec, 0, sizeof(Counters), s));
+	CVX_CUDA(cudaMemsetAsync(d_rec, 0, lay.big, s));  // counters and brick counts
 	return r.run(surf, solid);
 }
 
@@ -625,10 +677,16 @@ cvx_status cvx_voxelize_solid(const cvx_voxinfo* info, const float* d_tris, uint
 	return run_internal(surf, solid, (cudaStream_t)stream);
 }
 
+// Bricks of a single surface job on this voxinfo (0 if it does not use them).
+static uint32_t single_job_bricks(const cvx_voxinfo& v, int solid) {
+	const uint32_t g[3] = {v.gridsize[0], v.gridsize[1], v.gridsize[2]};
+	return (!solid && brick_grid(g)) ? bricks_of(g) : 0u;
+}
+
 uint64_t cvx_workspace_size(const cvx_voxinfo* info, int solid) {
 	if (!info) return 0;
 	const uint64_t n = std::max<uint64_t>(1, std::min<uint64_t>(info->n_triangles, kMaxTriPerLaunch));
-	const RecLayout lay = rec_layout(n, 0);
+	const RecLayout lay = rec_layout(n, 0, single_job_bricks(*info, solid));
 	uint64_t b = lay.end;
 	if (solid) b += align_up(words_of(*info) * 4);
 	return b;
@@ -649,7 +707,8 @@ cvx_status cvx_voxelize_ws(const cvx_voxinfo* info, const float* d_tris, uint32_
 	if (st != CVX_OK) return st;
 	cudaStream_t s = (cudaStream_t)stream;
 	const uint64_t cap = std::max<uint64_t>(1, std::min<uint64_t>(info->n_triangles, kMaxTriPerLaunch));
-	const RecLayout lay = rec_layout(cap, 0);
+	const uint32_t bricks = single_job_bricks(*info, solid);
+	const RecLayout lay = rec_layout(cap, 0, bricks);
 	char* rec = static_cast<char*>(d_ws);
 	std::vector<JobDesc> surf, sol;
 	JobDesc j = make_job(*info, d_tris, d_table, morton, solid);
@@ -660,10 +719,11 @@ cvx_status cvx_voxelize_ws(const cvx_voxinfo* info, const float* d_tris, uint32_
 	} else {
 		surf.push_back(j);
 	}
-	CVX_CUDA(cudaMemsetAsync(rec, 0, sizeof(Counters), s));
+	CVX_CUDA(cudaMemsetAsync(rec, 0, lay.big, s));  // counters and brick counts
 	Runner r{s, dev, rec, (size_t)lay.end, j.flips, nullptr, 0};
 	r.cap = cap;
 	r.jobs_off = lay.jobs;
+	r.bricks = bricks;
 	return r.run(surf, sol);
 }
 
@@ -744,9 +804,9 @@ constexpr int kPlanSurfaceLanes = 2;
 
 // One group's launches on a capturing stream, as Runner::run issues them but with the group's job
 // array (when it has more than one job) already resident at `jobs_dev`.
-static cudaError_t capture_group(const Group& g, bool solid, bool resolve, void* rec, uint64_t cap, JobDesc* jobs_dev,
-                          const DevState& dev, cudaStream_t s) {
-	const RecLayout l0 = rec_layout(cap, 0);
+static cudaError_t capture_group(const Group& g, bool solid, bool resolve, void* rec, uint64_t cap, uint32_t bricks,
+                                 JobDesc* jobs_dev, const DevState& dev, cudaStream_t s) {
+	if (g.bricks > bricks) return cudaErrorInvalidValue;
 	LaunchDesc L;
 	std::memset(&L, 0, sizeof(L));
 	L.n_jobs = (uint32_t)g.jobs.size();
@@ -756,10 +816,8 @@ static cudaError_t capture_group(const Group& g, bool solid, bool resolve, void*
 	L.n_mbricks = g.mbricks;
 	L.n_mslabs = g.mslabs;
 	L.slab_smem = g.slab_smem;
-	L.scr.ctr = reinterpret_cast<Counters*>(rec);
-	L.scr.big = reinterpret_cast<BigRec*>(static_cast<char*>(rec) + l0.big);
-	L.scr.mid = reinterpret_cast<MidRec*>(static_cast<char*>(rec) + l0.mid);
-	L.scr.cap = (uint32_t)cap;
+	L.n_bricks = g.bricks;
+	bind_scratch(L, static_cast<char*>(rec), cap, bricks, dev.tune);
 	if (g.jobs.size() == 1)
 		L.single = g.jobs[0];
 	else
@@ -768,7 +826,7 @@ static cudaError_t capture_group(const Group& g, bool solid, bool resolve, void*
 	const cudaError_t e = cudaMemsetAsync(rec, 0, kCountersResetBytes, s);
 	if (e != cudaSuccess) return e;
 	return solid ? launch_solid(L, dev.tune, dev.cols_grid, s, kSolidToggles, nullptr)
-	             : launch_surface(L, dev.tune, dev.rows_grid, s, nullptr);
+	             : launch_surface(L, dev.tune, dev.rows_grid, dev.raster_grid, s, nullptr);
 }
 
 cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out) {
@@ -800,6 +858,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		std::vector<JobDesc> jobs;
 		std::vector<Group> groups;  // toggles / surface launches; the solid lane's resolve is last
 		uint64_t cap = 1;
+		uint32_t bricks = 0;         // largest brick count of the lane's groups
 		size_t job_off = 0;          // first JobDesc slot of the lane in the job area
 		cudaStream_t stream = nullptr;
 		cudaEvent_t done = nullptr;
@@ -843,6 +902,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		for (size_t gi = 0; gi < l.groups.size(); gi++) {
 			const Group& g = l.groups[gi];
 			if (!(l.solid && gi + 1 == l.groups.size())) l.cap = std::max<uint64_t>(l.cap, g.tris);
+			if (!l.solid) l.bricks = std::max(l.bricks, g.bricks);
 			if (g.jobs.size() > 1) slots += g.jobs.size();
 		}
 	}
@@ -863,7 +923,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 	}
 	for (const Lane& l : lanes) {
 		void* rec = nullptr;
-		if (cudaMalloc(&rec, rec_layout(l.cap, 0).end) != cudaSuccess) {
+		if (cudaMalloc(&rec, rec_layout(l.cap, 0, l.bricks).end) != cudaSuccess) {
 			cudaGetLastError();
 			return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
 		}
@@ -927,7 +987,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		Lane& l = lanes[li];
 		void* rec = p->recs[li];
 		if ((fork && cudaStreamWaitEvent(l.stream, fork_ev, 0) != cudaSuccess) ||
-		    cudaMemsetAsync(rec, 0, sizeof(Counters), l.stream) != cudaSuccess) {
+		    cudaMemsetAsync(rec, 0, rec_layout(l.cap, 0, l.bricks).big, l.stream) != cudaSuccess) {
 			cst = cuda_fail(cudaGetLastError(), "capture lane");
 			break;
 		}
@@ -935,7 +995,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		for (size_t gi = 0; gi < l.groups.size() && cst == CVX_OK; gi++) {
 			const Group& g = l.groups[gi];
 			const bool resolve = l.solid && gi + 1 == l.groups.size();
-			const cudaError_t e = capture_group(g, l.solid, resolve, rec, l.cap, p->job_area + used, dev, l.stream);
+			const cudaError_t e = capture_group(g, l.solid, resolve, rec, l.cap, l.bricks, p->job_area + used, dev, l.stream);
 			if (g.jobs.size() > 1) used += g.jobs.size();
 			if (e != cudaSuccess) cst = cuda_fail(e, "capture launch");
 		}
@@ -1092,6 +1152,7 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 			steps.push_back(std::move(f));
 		}
 	uint64_t cap = 1;
+	uint32_t bricks = 0;
 	size_t slots = 0;
 	auto add_groups = [&](std::vector<JobDesc>& part, bool solid) {
 		if (part.empty()) return;
@@ -1100,6 +1161,7 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 			st.kind = HostStep::kLaunch;
 			st.solid = solid;
 			cap = std::max<uint64_t>(cap, g.tris);
+			if (!solid) bricks = std::max(bricks, g.bricks);
 			st.slot = slots;
 			if (g.jobs.size() > 1) slots += g.jobs.size();
 			st.g = std::move(g);
@@ -1169,7 +1231,7 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 			return bail(cuda_fail(cudaGetLastError(), "job upload"));
 	}
 	void* rec = nullptr;
-	if (cudaMalloc(&rec, rec_layout(cap, 0).end) != cudaSuccess) {
+	if (cudaMalloc(&rec, rec_layout(cap, 0, bricks).end) != cudaSuccess) {
 		cudaGetLastError();
 		return bail(fail(CVX_ERR_OUT_OF_MEMORY, "plan scratch"));
 	}
@@ -1238,7 +1300,7 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 		}
 	ck(cudaEventRecord(copied, cp), "capture upload");
 	for (uint32_t i = 0; i < n_jobs; i++) ck(cudaMemsetAsync(jobs[i].d_table, 0, words_of(jobs[i].info) * 4, cs), "capture clear");
-	ck(cudaMemsetAsync(rec, 0, sizeof(Counters), cs), "capture clear");
+	ck(cudaMemsetAsync(rec, 0, rec_layout(cap, 0, bricks).big, cs), "capture clear");
 	for (const HostStep& st : steps) {
 		if (cst != CVX_OK) break;
 		switch (st.kind) {
@@ -1247,7 +1309,7 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 			break;
 		case HostStep::kLaunch:
 		case HostStep::kResolve:
-			ck(capture_group(st.g, st.solid, st.kind == HostStep::kResolve, rec, cap, p->job_area + st.slot, dev, cs),
+			ck(capture_group(st.g, st.solid, st.kind == HostStep::kResolve, rec, cap, bricks, p->job_area + st.slot, dev, cs),
 			   "capture launch");
 			break;
 		case HostStep::kFinal: {
@@ -1326,6 +1388,7 @@ cvx_status cvx_get_tuning(int device, cvx_tuning* out) {
 	if (it != g_dev.end()) t = it->second.tune;
 	out->small_vox = t.small_vox;
 	out->small_cols = t.small_cols;
+	out->brick_pairs = t.brick_pairs;
 	return CVX_OK;
 }
 
@@ -1341,6 +1404,7 @@ cvx_status cvx_set_tuning(int device, const cvx_tuning* in) {
 	std::lock_guard<std::mutex> lk(g_mu);
 	g_dev[device].tune.small_vox = in->small_vox;
 	g_dev[device].tune.small_cols = in->small_cols;
+	g_dev[device].tune.brick_pairs = std::min(in->brick_pairs, kMaxBrickPairs);
 	return CVX_OK;
 }
 

@@ -10,6 +10,7 @@
 // re-organisation the engine does (row intervals, column queues, parity flips) only changes
 // *which* voxels are evaluated and in what order, never the value of a predicate at a voxel.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -74,7 +75,10 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 // JOB_PLAIN_LOADS: the job's triangles are not plain device memory (managed, host-registered or
 // system memory -- the reference's main() passes cudaMallocManaged buffers): the classify kernels
 // read them with ordinary loads instead of bulk copies.
-enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u, JOB_TABLE_ZERO = 8u, JOB_PLAIN_LOADS = 16u };
+// JOB_BRICKS: a surface job whose queued (larger) triangles are rasterized brick by brick in shared
+// memory (bricks.cu) instead of by per-row global atomics.
+enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u, JOB_TABLE_ZERO = 8u, JOB_PLAIN_LOADS = 16u,
+                  JOB_BRICKS = 32u };
 
 // One mesh voxelization.  Plain data, uploaded as an array for batches or passed by value for a
 // single mesh.
@@ -93,6 +97,8 @@ struct JobDesc {
 	uint64_t mword_begin;  // solid Morton, g < 32: first Morton word in the launch's word space
 	uint64_t mbrick_begin; // solid Morton, g > 1024: first group of x-adjacent 32^3 bricks in the launch
 	uint64_t mslab_begin;  // solid Morton, 32 <= g <= 1024: first 16x16-row slab in the launch
+	uint32_t brick_begin;  // JOB_BRICKS: first 32^3 brick of this job in the launch's brick space
+	uint32_t pad;
 };
 
 // Work-queue records written by the classify kernels and consumed by the cooperative kernels.
@@ -114,11 +120,18 @@ constexpr unsigned long long kBigItemMask = (1ull << kBigShift) - 1ull;
 struct Counters {
 	unsigned long long big;
 	unsigned long long ticket;   // next work ticket of the cooperative kernel
+	unsigned long long pairs;    // (brick, triangle) pairs reserved by brick_bin
+	unsigned long long bticket;  // next triangle of the brick queue for brick_bin
+	unsigned long long fticket;  // next triangle of the brick queue for brick_fill
+	unsigned long long rticket;  // next raster work unit for brick_raster
 	unsigned int mid;            // number of MidRec
+	unsigned int bq;             // number of triangles in the brick queue
+	unsigned int units;          // raster work units (written by brick_scan)
 	unsigned int error;          // nonzero: a device-side check failed (value says which)
 	unsigned int pad[2];
 };
-constexpr size_t kCountersResetBytes = 20;  // big, ticket, mid: reset before every launch sequence
+// Everything before `error` is reset before every launch sequence; `error` persists until read.
+constexpr size_t kCountersResetBytes = offsetof(Counters, error);
 
 // Work tickets of the cooperative kernels, claimed by a warp K at a time: one atomic on the shared
 // counter per K items instead of per item (a single hot address serialises in its L2 slice when
@@ -147,11 +160,37 @@ struct WarpTickets {
 	}
 };
 
+// Brick rasterization (JOB_BRICKS jobs, bricks.cu): the queued triangles of those jobs are binned to
+// the 32^3 bricks of their tables that their planes cross, the (brick, triangle) pairs are grouped
+// by brick with a counting sort, and each warp rasterizes a brick's pairs into a brick of its own in
+// shared memory, then ORs it into the table with one global atomic per nonzero word.
+constexpr uint32_t kBrickShift = 5;
+constexpr uint32_t kBrick = 1u << kBrickShift;                       // voxels per brick edge
+constexpr uint32_t kBrickWords = kBrick * kBrick * kBrick / 32u;      // 1024 words = 4 KiB per warp
+constexpr uint32_t kPairsPerUnit = 256;                                // pairs per raster work unit
+
+// A queued triangle's setup, cached by brick_bin for brick_fill and brick_raster (176 bytes).
+struct __align__(16) BrickTri {
+	float f[35];      // nx ny nz d1 d2, exy[3][2] eyz[3][2] ezx[3][2], dxy[3] dyz[3] dzx[3], v0.xyz
+	int bb[6];        // bx0 by0 bz0 bx1 by1 bz1
+	uint32_t binned;  // 1: its pairs are in the pair area; 0: surf_rows rasterizes it
+	uint32_t pad[2];
+};
+static_assert(sizeof(BrickTri) == 176, "BrickTri is eleven 16-byte vectors");
+
 struct Scratch {
 	Counters* ctr;
 	BigRec* big;
 	MidRec* mid;
-	uint32_t cap;          // capacity of big[] and mid[] (>= triangles in the launch)
+	uint32_t cap;          // capacity of big[], mid[], bq[] and tri[] (>= triangles in the launch)
+	uint32_t pair_cap;     // capacity of pair_sorted (0: no pair area, every triangle goes to surf_rows)
+	MidRec* bq;            // triangles of JOB_BRICKS jobs queued by the classify kernel
+	BrickTri* tri;         // their setups, in queue order
+	uint32_t* brick_cnt;   // pairs per brick (zero between launch sequences: brick_scan clears what it read)
+	uint32_t* brick_off;   // n_bricks + 1: first sorted pair of each brick
+	uint32_t* brick_cur;   // fill cursors
+	uint32_t* unit_begin;  // n_bricks + 1: first raster work unit of each brick
+	uint32_t* pair_sorted; // queue index of each pair's triangle, grouped by brick
 };
 
 struct LaunchDesc {
@@ -164,7 +203,7 @@ struct LaunchDesc {
 	uint64_t n_mbricks;    // groups of x-adjacent 32^3 bricks of solid Morton jobs with g > 1024
 	uint64_t n_mslabs;     // 16x16-row slabs of solid Morton jobs with 32 <= g <= 1024
 	uint32_t slab_smem;    // dynamic shared memory of the slab kernel (largest slab of the launch)
-	uint32_t pad2;
+	uint32_t n_bricks;     // 32^3 bricks of the launch's JOB_BRICKS jobs
 	Scratch scr;
 };
 

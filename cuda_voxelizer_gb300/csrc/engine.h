@@ -25,9 +25,14 @@ enum : unsigned { kErrBulkTimeout = 1u, kErrQueueOverflow = 2u };
 constexpr uint64_t kMaxTriPerLaunch = (1ull << 24) - 1;
 
 // Tunables (picked per device by the autotuner; defaults are safe everywhere).
+// Pair area of the brick rasterizer: room for this many (brick, triangle) pairs per triangle of a
+// launch (about 27 per queued triangle, 12.5 per triangle, on the 1024^3 stress soup).
+constexpr uint32_t kMaxBrickPairs = 16;
+
 struct Tune {
 	uint32_t small_vox = 64;    // surface: bbox voxels at or below which a triangle stays in its thread
 	uint32_t small_cols = kSmallCols;  // solid: columns at or below which a triangle stays in the classify kernel
+	uint32_t brick_pairs = kMaxBrickPairs;  // pairs per triangle the brick rasterizer may use (0: rows only)
 };
 
 // Optional per-kernel timing: mark(name) records an event on the stream after the named kernel
@@ -56,9 +61,26 @@ inline cudaError_t launch_after(void (*kernel)(KArgs...), unsigned grid, unsigne
 	return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
-// Surface launch sequence: classify + cooperative rows.  Counters must be zero.
-cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s, const Prof* prof);
+// Surface launch sequence: classify, then (when the launch has JOB_BRICKS jobs, L.n_bricks > 0) the
+// brick kernels, then the cooperative rows.  Counters must be zero.
+cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, int raster_grid, cudaStream_t s,
+                           const Prof* prof);
 int surf_rows_blocks_per_sm();
+
+// The brick kernels of a surface launch sequence (bricks.cu): bin, scan, scatter, raster.
+cudaError_t launch_bricks(const LaunchDesc& L, int grid, int raster_grid, cudaStream_t s, const Prof* prof);
+int brick_raster_blocks_per_sm();
+
+// A surface job rasterizes its larger triangles in bricks when its table is larger than the L2 cache
+// can hold beside other work (at least 2^29 voxels, 64 MiB: smaller tables stay in L2, where
+// per-row atomics are cheap) and every axis is at most 2048 (bounds the bricks one triangle's bbox
+// can span).
+inline bool brick_grid(const uint32_t g[3]) {
+	return (uint64_t)g[0] * g[1] * g[2] >= (1ull << 29) && g[0] <= 2048 && g[1] <= 2048 && g[2] <= 2048;
+}
+inline uint32_t bricks_of(const uint32_t g[3]) {
+	return ((g[0] + kBrick - 1) >> kBrickShift) * ((g[1] + kBrick - 1) >> kBrickShift) * ((g[2] + kBrick - 1) >> kBrickShift);
+}
 
 // Solid launch sequence.  kSolidToggles: classify + cooperative columns (counters must be zero);
 // kSolidResolve: prefix-XOR resolve into the tables (+ Morton transcode).  Every job's flips table

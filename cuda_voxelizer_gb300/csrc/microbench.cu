@@ -1,6 +1,7 @@
 // microbench.cu -- device peak measurements the roofline needs and MEASURED_PEAKS.json lacks:
 // the rate of 32-bit global atomicOr into a large table (L2 atomic throughput), for the access
-// patterns the voxelizer produces.  Built into libcvx.so; used by bench.py.
+// patterns the voxelizer produces.  Built into its own library, libcvx_diag.so (include/cvx_diag.h),
+// apart from the voxelization library; used by bench.py.
 //
 //   pattern 0: every lane hits a pseudo-random word of the table (scattered, distinct lines)
 //   pattern 1: each warp hits 32 consecutive words (one 128-byte line per warp instruction)
@@ -8,7 +9,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
-#include "cvx.h"
+#include "cvx_diag.h"
 
 namespace {
 

@@ -119,22 +119,21 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 	__shared__ uint32_t s_warp[kTile / 32];
 	__shared__ uint32_t s_fit;  // end of the item list: the first local triangle that did not fit
 	__shared__ __align__(8) uint64_t s_bar;
-	pdl_trigger();  // surf_rows may be scheduled as this grid's last wave runs
+	pdl_trigger();  // the next kernel may be scheduled as this grid's last wave runs
 	const uint32_t tile = blockIdx.x;
 	const uint32_t j = job_of_tile(L, tile);
 	const JobDesc& J = job_at(L, j);
 	const float* tris = J.tris;
 	uint32_t* table = J.table;
 	const uint64_t n = J.n_tri;
-	const bool morton = (J.flags & JOB_MORTON) != 0;
-	const bool narrow = (J.flags & JOB_NARROW) != 0;
+	const uint32_t jflags = J.flags;
 	const float bmin[3] = {J.bmin[0], J.bmin[1], J.bmin[2]};
 	const float unit[3] = {J.unit[0], J.unit[1], J.unit[2]};
 	const float inv[3] = {J.inv_unit[0], J.inv_unit[1], J.inv_unit[2]};
 	const uint32_t grid[3] = {J.grid[0], J.grid[1], J.grid[2]};
 	const uint64_t t0 = (uint64_t)(tile - J.tile_begin) * kTile;
 	const uint32_t cnt = (uint32_t)umin64((uint64_t)kTile, n - t0);
-	if (!stage_tile(L, tris + t0 * 9, cnt, sm.tri, &s_bar, (J.flags & JOB_PLAIN_LOADS) != 0)) return;  // tile not staged: error word set
+	if (!stage_tile(L, tris + t0 * 9, cnt, sm.tri, &s_bar, (jflags & JOB_PLAIN_LOADS) != 0)) return;  // tile not staged: error word set
 
 	const uint32_t lane = threadIdx.x & 31u;
 	const bool valid = threadIdx.x < cnt;
@@ -173,12 +172,29 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 		atomicMin(&s_fit, loff);
 		n_local = 0;
 	}
+	bool is_brick = false;
 	if (n_items && !n_local) {
-		is_mid = n_items == 1;
-		is_big = n_items > 1;
+		if (jflags & JOB_BRICKS) {
+			is_brick = true;  // rasterized in shared-memory bricks (bricks.cu)
+		} else {
+			is_mid = n_items == 1;
+			is_big = n_items > 1;
+		}
 	}
 	// Queue the other triangles: warp-aggregated appends.
 	const uint32_t lt = (1u << lane) - 1u;
+	const uint32_t brick_ballot = __ballot_sync(FULL, is_brick);
+	if (brick_ballot) {
+		uint32_t base = 0;
+		const uint32_t leader = __ffs(brick_ballot) - 1;
+		if (lane == leader) base = atomicAdd(&L.scr.ctr->bq, (unsigned)__popc(brick_ballot));
+		base = __shfl_sync(FULL, base, leader);
+		const uint32_t slot = base + __popc(brick_ballot & lt);
+		if (is_brick) {
+			if (slot < L.scr.cap) L.scr.bq[slot] = MidRec{j, (uint32_t)(t0 + threadIdx.x)};
+			else set_error(L, kErrQueueOverflow);
+		}
+	}
 	const uint32_t mid_ballot = __ballot_sync(FULL, is_mid);
 	if (mid_ballot) {
 		uint32_t base = 0;
@@ -253,12 +269,13 @@ __global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant_
 			// src/voxelize.cu:136-183: every voxel of the row (at most 16), as a pass mask
 			uint32_t pm = 0;
 			for (int i = 0; i <= S.bx1 - S.bx0; i++) pm |= (uint32_t)voxel_pass<P>(S, K, unit[0], S.bx0 + i) << i;
-			if (pm) write_row_mask(table, morton, narrow, grid, y, z, S.bx0, pm);
+			if (pm) write_row_mask(table, (jflags & JOB_MORTON) != 0, (jflags & JOB_NARROW) != 0, grid, y, z, S.bx0, pm);
 		} else {
 			RowDirs D;
 			row_dirs(S, unit[0], D);
 			int xl, xh;
-			if (row_interval<P>(S, D, K, unit[0], xl, xh)) write_row(table, morton, narrow, grid, y, z, xl, xh);
+			if (row_interval<P>(S, D, K, unit[0], xl, xh))
+				write_row(table, (jflags & JOB_MORTON) != 0, (jflags & JOB_NARROW) != 0, grid, y, z, xl, xh);
 		}
 	}
 }
@@ -367,7 +384,7 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 				const float pz = __fmul_rn(__int2float_rn(z), unit[2]);
 				RowK K;
 				row_consts<P>(S, py, pz, K);
-				if (!row_interval<P>(S, D, K, unit[0], xl, xh)) xh = -1;
+				if (!row_interval_fast<P>(S, D, K, unit[0], S.bx0, S.bx1, xl, xh)) xh = -1;
 			}
 			// Short rows are written by their own lane.  Long rows are written by the whole warp, one
 			// row at a time with the lanes on consecutive words (linear) or x groups (Morton): a
@@ -393,22 +410,27 @@ __global__ void __launch_bounds__(kRowsThreads) surf_rows(const __grid_constant_
 // ---- host-side launchers ------------------------------------------------------------------------
 
 template <class P>
-static cudaError_t launch_surface_t(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s,
-                                    const Prof* prof) {
+static cudaError_t launch_surface_t(const LaunchDesc& L, const Tune& tune, int rows_grid, int raster_grid,
+                                    cudaStream_t s, const Prof* prof) {
 	if (L.n_tiles == 0) return cudaSuccess;
 	if (prof) (*prof)(nullptr, s);
 	surf_classify<P><<<L.n_tiles, kTile, 0, s>>>(L, tune.small_vox);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("surf_classify", s);
+	if (L.n_bricks) {  // with no pair area (pair_cap 0) brick_bin queues every triangle for surf_rows
+		e = launch_bricks(L, rows_grid, raster_grid, s, prof);
+		if (e != cudaSuccess) return e;
+	}
 	e = launch_after(surf_rows<P>, (unsigned)rows_grid, kRowsThreads, 0, s, L);
 	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("surf_rows", s);
 	return cudaGetLastError();
 }
 
-cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, cudaStream_t s, const Prof* prof) {
-	return launch_surface_t<RefFma>(L, tune, rows_grid, s, prof);
+cudaError_t launch_surface(const LaunchDesc& L, const Tune& tune, int rows_grid, int raster_grid, cudaStream_t s,
+                           const Prof* prof) {
+	return launch_surface_t<RefFma>(L, tune, rows_grid, raster_grid, s, prof);
 }
 
 int surf_rows_blocks_per_sm() {

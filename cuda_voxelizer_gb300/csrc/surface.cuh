@@ -262,12 +262,12 @@ __device__ __forceinline__ float crossing(const SurfTri& S, const RowDirs& D, fl
 	return (S.ezx[i - 5][0] * pz + S.dzx[i - 5]) * D.inv[i];
 }
 
-// Exact pass interval of row (y, z) within [bx0, bx1].  Returns false if the row is empty.
-// Correct for any estimate quality: the estimates only choose where the exact walk starts.
+// Exact pass interval of row (y, z) within [bx0, bx1] (a sub-range of the triangle's bbox: each
+// test is monotone on any range).  Returns false if the row is empty.  Correct for any estimate
+// quality: the estimates only choose where the exact walk starts.
 template <class P>
-__device__ __forceinline__ bool row_interval(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int& xl,
-                                             int& xh) {
-	const int bx0 = S.bx0, bx1 = S.bx1;
+__device__ __forceinline__ bool row_interval_in(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int bx0,
+                                                int bx1, int& xl, int& xh) {
 	const uint32_t cmask = ~(D.lo | D.hi) & 0xFFu;
 	// tests that do not depend on x: evaluate once
 	if (cmask && (fail_bits<P>(S, K, ux, bx0) & cmask)) return false;
@@ -303,12 +303,169 @@ __device__ __forceinline__ bool row_interval(const SurfTri& S, const RowDirs& D,
 	return true;
 }
 
-// Pass interval of the YZ tests along y for a fixed z slice, within [by0, by1] (same scheme:
-// every YZ test is monotone in p.y).
+// The x-dependent tests selected by `mask` at voxel x (bit i set = test i fails; bit layout of
+// fail_bits).  For callers whose mask is the same in every lane of a warp (one triangle per warp),
+// the tests outside the mask cost a uniform branch each instead of their evaluation.
 template <class P>
-__device__ __forceinline__ bool y_interval(const SurfTri& S, float uy, float pz, int& ya, int& yb) {
+__device__ __forceinline__ uint32_t fail_bits_masked(const SurfTri& S, const RowK& K, float ux, int x, uint32_t mask) {
+	const float px = __fmul_rn(__int2float_rn(x), ux);
+	uint32_t f = 0;
+	if (mask & 3u) {
+		float s;
+		if constexpr (P::plane == 1) s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.nx, px, K.kpl));
+		else if constexpr (P::plane == 2) s = __fadd_rn(__fmaf_rn(S.nx, px, K.kpl), K.kpl2);
+		else if constexpr (P::plane == 3) s = __fmaf_rn(S.nz, K.pz, __fmaf_rn(S.ny, K.py, __fmul_rn(S.nx, px)));
+		else s = __fadd_rn(__fadd_rn(__fmul_rn(S.nx, px), K.kpl), K.kpl2);
+		const float a = __fadd_rn(s, S.d1), b = __fadd_rn(s, S.d2);
+		const bool pf = __fmul_rn(a, b) > 0.0f;
+		f = (pf && a < 0.0f ? 1u : 0u) | (pf && a > 0.0f ? 2u : 0u);
+	}
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		if (mask & (4u << i)) {
+			float v;
+			if constexpr (P::edge_xy == 1) v = __fmaf_rn(S.exy[i][0], px, K.kxy[i]);
+			else v = mul_add<P::edge_xy>(S.exy[i][0], px, S.exy[i][1], K.py);
+			f |= (__fadd_rn(v, S.dxy[i]) < 0.0f ? 4u : 0u) << i;
+		}
+	}
+#pragma unroll
+	for (int i = 0; i < 3; i++) {
+		if (mask & (32u << i)) {
+			float v;
+			if constexpr (P::edge_zx == 2) v = __fmaf_rn(S.ezx[i][1], px, K.kzx[i]);
+			else v = mul_add<P::edge_zx>(S.ezx[i][0], K.pz, S.ezx[i][1], px);
+			f |= (__fadd_rn(v, S.dzx[i]) < 0.0f ? 32u : 0u) << i;
+		}
+	}
+	return f & mask;
+}
+
+// row_interval_in for callers whose RowDirs are warp-uniform (one triangle per warp): each end
+// evaluates only the tests that bound it (lower-bound tests at the lower end, upper-bound tests at
+// the upper end).  Same result: an end is fixed by its own tests alone.
+template <class P>
+__device__ __forceinline__ bool row_interval_split(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int bx0,
+                                                   int bx1, int& xl, int& xh) {
+	const uint32_t dep = D.lo | D.hi;
+	const uint32_t cmask = ~dep & 0xFFu;
+	if (cmask && fail_bits_masked<P>(S, K, ux, bx0, cmask)) return false;
+	float elo = (float)bx0, ehi = (float)bx1;
+#pragma unroll
+	for (int i = 0; i < 8; i++) {
+		const uint32_t bit = 1u << i;
+		if (dep & bit) {
+			const float c = crossing(S, D, K.py, K.pz, i);
+			if (D.lo & bit) elo = fmaxf(elo, ceilf(c));
+			else ehi = fminf(ehi, floorf(c));
+		}
+	}
+	int e = (int)fminf(fmaxf(elo, (float)bx0), (float)bx1);
+	if (D.lo) {
+		if (!fail_bits_masked<P>(S, K, ux, e, D.lo)) {
+			while (e > bx0 && !fail_bits_masked<P>(S, K, ux, e - 1, D.lo)) e--;
+		} else {
+			do { e++; } while (e <= bx1 && fail_bits_masked<P>(S, K, ux, e, D.lo));
+			if (e > bx1) return false;
+		}
+	}
+	xl = e;
+	int f = (int)fminf(fmaxf(ehi, (float)xl), (float)bx1);
+	if (D.hi) {
+		if (!fail_bits_masked<P>(S, K, ux, f, D.hi)) {
+			while (f < bx1 && !fail_bits_masked<P>(S, K, ux, f + 1, D.hi)) f++;
+		} else {
+			do { f--; } while (f >= xl && fail_bits_masked<P>(S, K, ux, f, D.hi));
+			if (f < xl) return false;
+		}
+	}
+	xh = f;
+	return true;
+}
+
+// Exact pass interval of row (y, z) within the triangle's bbox [S.bx0, S.bx1].
+template <class P>
+__device__ __forceinline__ bool row_interval(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int& xl,
+                                             int& xh) {
+	return row_interval_in<P>(S, D, K, ux, S.bx0, S.bx1, xl, xh);
+}
+
+// Certified x-interval of a row, without walking.
+//
+// Each x-dependent test i has the form "fails iff g(x) < 0" (or > 0 for the plane's "above" side)
+// with g(x) = fl(fl(fl(fma(a, fl(x * ux), k1)) + k2) + d): a the test's coefficient of x, k1 and k2
+// the row constants (k2 = 0 for the edge tests), d the triangle constant.  Its real counterpart
+// G(x) = a*ux*x + k1 + k2 + d is linear with root x* = -(k1 + k2 + d) / (a * ux).  Rounding moves
+// each intermediate by at most u = 2^-24 relative, and the last rounding preserves the sign, so
+// sign(g(x)) = sign(G(x) + E) with |E| <= 3.01u (|a ux x| + |k1| + |k2|): the float test agrees with
+// the real one at every integer x with |x - x*| > W = 3.01u (|x| + (|k1| + |k2|) / |a ux|).  The
+// estimate xe = fl(fl(k1 + k2 + d) * inv), inv the fast reciprocal of -a * ux, is within
+// 2.01u (|k1| + |k2| + |d|) |inv| + 5u |xe| of x*.  So with the band
+//     B = 2^-20 (|xe| + (|k1| + |k2| + |d|) |inv| + 1)  >=  W + |xe - x*| + the rounding of xe +- B,
+// every integer outside [xe - B, xe + B] is decided like the real test; when B < 1/4 the band holds
+// at most one integer, and that one is decided by evaluating the float test there.  The plane's two
+// sides use a = fl(s + d1) and b = fl(s + d2) with the same s: for d1 >= d2 rounding keeps b <= a,
+// so "below" fails iff a < 0 and "above" iff b > 0, except when the product a * b underflows, which
+// needs |a| < 2^-75 and cannot happen outside the band while |n.x * ux| >= 2^-40.  The lower end is
+// the largest first-passing x of the tests that pass on a suffix, the upper end the smallest last-
+// passing x of those that pass on a prefix.  Identical to row_interval_in wherever it answers; it
+// declines (returns 2) for x-independent tests, d1 < d2, crossings beyond 2^22 voxels or bands of a
+// quarter voxel and more, and the caller then uses row_interval_in.  Returns 1 with [xl, xh] set,
+// or 0 for an empty row.
+template <class P>
+__device__ __forceinline__ int row_interval_cert(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int bx0,
+                                                 int bx1, int& xl, int& xh) {
+	static_assert(P::plane == 2 && P::edge_xy == 1 && P::edge_zx == 2,
+	              "the certified row interval follows the pinned fused-multiply-add pattern");
+	if (((D.lo | D.hi) & 0xFFu) != 0xFFu || !(S.d1 >= S.d2) || !(fabsf(D.inv[0]) <= 1e12f)) return 2;
+	constexpr float kBand = 0x1p-20f;
+	float lo = (float)bx0, hi = (float)bx1;
+	bool ok = true;
+	const float kp = __fadd_rn(K.kpl, K.kpl2), mp = fabsf(K.kpl) + fabsf(K.kpl2);
+#pragma unroll
+	for (int i = 0; i < 8; i++) {
+		float t, m;
+		if (i == 0) { t = __fadd_rn(kp, S.d1); m = mp + fabsf(S.d1); }
+		else if (i == 1) { t = __fadd_rn(kp, S.d2); m = mp + fabsf(S.d2); }
+		else if (i < 5) { t = __fadd_rn(K.kxy[i - 2], S.dxy[i - 2]); m = fabsf(K.kxy[i - 2]) + fabsf(S.dxy[i - 2]); }
+		else { t = __fadd_rn(K.kzx[i - 5], S.dzx[i - 5]); m = fabsf(K.kzx[i - 5]) + fabsf(S.dzx[i - 5]); }
+		const float inv = D.inv[i];
+		const float xe = __fmul_rn(t, inv);
+		const float B = kBand * (fabsf(xe) + m * fabsf(inv) + 1.0f);
+		ok = ok && fabsf(xe) < 4194304.0f && B < 0.25f && inv != 0.0f;  // false for NaN too
+		const bool is_lo = (D.lo >> i) & 1u;
+		const float c = is_lo ? ceilf(xe - B) : floorf(xe + B);  // the one integer the band may hold
+		float e = c;
+		if (ok && (is_lo ? c < xe + B : c > xe - B)) {
+			const bool fails = fail_bits_masked<P>(S, K, ux, (int)c, 1u << i) != 0u;
+			e = is_lo ? (fails ? c + 1.0f : c) : (fails ? c - 1.0f : c);
+		}
+		if (is_lo) lo = fmaxf(lo, e); else hi = fminf(hi, e);
+	}
+	if (!ok) return 2;
+	if (lo > hi) return 0;
+	xl = (int)lo;
+	xh = (int)hi;
+	return 1;
+}
+
+// Exact x-interval of a row within [bx0, bx1]: the certified computation, or the walk where that
+// declines.
+template <class P>
+__device__ __forceinline__ bool row_interval_fast(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int bx0,
+                                                  int bx1, int& xl, int& xh) {
+	const int r = row_interval_cert<P>(S, D, K, ux, bx0, bx1, xl, xh);
+	if (r != 2) return r == 1;
+	return row_interval_in<P>(S, D, K, ux, bx0, bx1, xl, xh);
+}
+
+// Pass interval of the YZ tests along y for a fixed z slice, within [by0, by1] (a sub-range of the
+// triangle's bbox; same scheme: every YZ test is monotone in p.y).
+template <class P>
+__device__ __forceinline__ bool y_interval_in(const SurfTri& S, float uy, float pz, int by0, int by1, int& ya,
+                                              int& yb) {
 	uint32_t lo = 0, hi = 0;
-	float elo = (float)S.by0, ehi = (float)S.by1;
+	float elo = (float)by0, ehi = (float)by1;
 #pragma unroll
 	for (int i = 0; i < 3; i++) {
 		const float a = S.eyz[i][0];
@@ -320,24 +477,29 @@ __device__ __forceinline__ bool y_interval(const SurfTri& S, float uy, float pz,
 	}
 	const uint32_t cmask = ~(lo | hi) & 7u;
 	auto fails = [&](int y) { return yz_fail_bits<P>(S, __fmul_rn(__int2float_rn(y), uy), pz); };
-	if (cmask && (fails(S.by0) & cmask)) return false;
-	int e = (int)fminf(fmaxf(elo, (float)S.by0), (float)S.by1);
+	if (cmask && (fails(by0) & cmask)) return false;
+	int e = (int)fminf(fmaxf(elo, (float)by0), (float)by1);
 	if (!(fails(e) & lo)) {
-		while (e > S.by0 && !(fails(e - 1) & lo)) e--;
+		while (e > by0 && !(fails(e - 1) & lo)) e--;
 	} else {
-		do { e++; } while (e <= S.by1 && (fails(e) & lo));
-		if (e > S.by1) return false;
+		do { e++; } while (e <= by1 && (fails(e) & lo));
+		if (e > by1) return false;
 	}
 	ya = e;
-	int f = (int)fminf(fmaxf(ehi, (float)ya), (float)S.by1);
+	int f = (int)fminf(fmaxf(ehi, (float)ya), (float)by1);
 	if (!(fails(f) & hi)) {
-		while (f < S.by1 && !(fails(f + 1) & hi)) f++;
+		while (f < by1 && !(fails(f + 1) & hi)) f++;
 	} else {
 		do { f--; } while (f >= ya && (fails(f) & hi));
 		if (f < ya) return false;
 	}
 	yb = f;
 	return true;
+}
+
+template <class P>
+__device__ __forceinline__ bool y_interval(const SurfTri& S, float uy, float pz, int& ya, int& yb) {
+	return y_interval_in<P>(S, uy, pz, S.by0, S.by1, ya, yb);
 }
 
 // The writers below come in two code types C: uint64_t in general, uint32_t for JOB_NARROW jobs

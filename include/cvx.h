@@ -30,7 +30,7 @@ extern "C" {
 #endif
 
 #define CVX_VERSION_MAJOR 1
-#define CVX_VERSION_MINOR 0
+#define CVX_VERSION_MINOR 1
 
 /* Same bytes as the reference's voxinfo (src/util.h:50-69) on LP64 targets:
  * AABox<float3> bbox @0, uint3 gridsize @24, size_t n_triangles @40, float3 unit @48, 64 bytes. */
@@ -268,6 +268,9 @@ cvx_status cvx_encode_voxel_list(const cvx_voxinfo* info, const uint32_t* d_tabl
 typedef struct cvx_tuning {
 	uint32_t small_vox;   /* surface: triangles with at most this many bbox voxels stay in one thread */
 	uint32_t small_cols;  /* solid: triangles with at most this many columns stay in one thread */
+	uint32_t brick_pairs; /* surface, grids of 2^29+ voxels: (brick, triangle) pairs per triangle the
+	                       * shared-memory brick rasterizer may use, at most 16; 0 rasterizes every
+	                       * larger triangle row by row with global atomics instead */
 } cvx_tuning;
 /* Per-device tuning used by subsequent calls (results never depend on it). */
 cvx_status cvx_get_tuning(int device, cvx_tuning* out);
@@ -280,12 +283,6 @@ cvx_status cvx_set_tuning(int device, const cvx_tuning* in);
  * name, milliseconds) pairs in launch order and forgets them.  Names are static strings. */
 cvx_status cvx_profile_enable(int on);
 int cvx_profile_collect(const char** names, float* ms, int max_entries);
-
-/* ---- peak measurement for the roofline ------------------------------------------------------- */
-
-/* 32-bit global atomicOr per second into d_table (words long): pattern 0 scattered lanes,
- * 1 one 128-byte line per warp, 2 eight consecutive words per lane.  Synchronous. */
-double cvx_microbench_atomic_or(uint32_t* d_table, uint64_t words, int pattern, uint32_t blocks, uint32_t iters);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -34,6 +34,12 @@ def test_every_declared_function_is_exported(name):
     assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
 
 
+def test_diagnostics_library_is_separate():
+    # the atomicOr-rate measurement (include/cvx_diag.h) lives in libcvx_diag.so, not in the ABI library
+    assert not hasattr(_lib.lib, "cvx_microbench_atomic_or")
+    assert hasattr(_lib.diag_lib(), "cvx_microbench_atomic_or")
+
+
 def test_dropin_cxx_symbols_exported():
     # void voxelize(const voxinfo&, float*, unsigned int*, bool) and voxelize_solid(...), C++ linkage
     for sym in ("_Z8voxelizeRK7voxinfoPfPjb", "_Z14voxelize_solidRK7voxinfoPfPjb"):

@@ -40,12 +40,13 @@ def test_autotune_applies_and_caches(tmp_path):
     path = str(tmp_path / "tuning.json")
     try:
         r = at.autotune(0, cache_path=path, reps=2)
-        assert cv.get_tuning(0) == {"small_vox": r["small_vox"], "small_cols": r["small_cols"]}
+        choice = {k: r[k] for k in at.KNOBS}
+        assert cv.get_tuning(0) == choice
         assert r["ms"] <= min(c["ms"] for c in r["candidates"]) + 1e-9
         with open(path) as f:
-            assert json.load(f)[r["device"]] == {"small_vox": r["small_vox"], "small_cols": r["small_cols"]}
+            assert json.load(f)[r["device"]] == choice
         cv.set_tuning(0, **before)
-        assert at.load_cached(0, path) == {"small_vox": r["small_vox"], "small_cols": r["small_cols"]}
-        assert cv.get_tuning(0)["small_vox"] == r["small_vox"]
+        assert at.load_cached(0, path) == choice
+        assert cv.get_tuning(0) == choice
     finally:
         cv.set_tuning(0, **before)

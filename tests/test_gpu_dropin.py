@@ -123,6 +123,7 @@ def test_cxx_symbols_on_managed_memory(ref, capfd, name, morton, solid):
     with Managed(rt, tris.nbytes) as mt, Managed(rt, 4 * words) as mv:
         mt.write(tris)
         _symbol(SYM_SOLID if solid else SYM_SURFACE)(ctypes.byref(info), mt.ptr, mv.ptr, morton)
+        ctypes.CDLL(None).fflush(None)  # the [Perf] line is a buffered printf, as in the reference
         out = capfd.readouterr().out
         got = mv.read_u32(words)  # the call synchronized the device: host reads are safe
         assert "[Perf] Voxelization GPU time:" in out, out
