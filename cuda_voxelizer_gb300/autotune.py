@@ -3,7 +3,7 @@
 The knobs decide where a triangle's work goes; results never depend on them, only the time does:
 ``small_vox`` (surface: triangles whose grid bounding box holds at most this many voxels are tested
 voxel by voxel in the classify kernel), ``small_cols`` (solid: triangles with at most this many
-voxel-centre columns stay in the classify kernel) and ``brick_pairs`` (surface, grids of 2^24+
+voxel-centre columns stay in the classify kernel) and ``brick_pairs`` (surface, grids of 2^29+
 voxels: (brick, triangle) pairs per triangle the shared-memory brick rasterizer may use; 0 sends
 every larger triangle to the row-by-row path with global atomics).  ``autotune()`` times a fixed set
 of seeded workloads -- sub-voxel and few-voxel triangles at several grids, surface and solid, linear
@@ -27,7 +27,7 @@ from . import meshgen
 
 SMALL_VOX = (16, 32, 64, 128, 255)
 SMALL_COLS = (4, 8, 16)
-BRICK_PAIRS = (0, 8)
+BRICK_PAIRS = (0, 16)
 KNOBS = ("small_vox", "small_cols", "brick_pairs")
 DEFAULT_CACHE = os.environ.get("CVX_TUNING_CACHE") or os.path.join(os.path.expanduser("~"), ".cache",
                                                                      "cuda_voxelizer_gb300", "tuning.json")

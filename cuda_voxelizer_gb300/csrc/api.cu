@@ -244,6 +244,18 @@ cvx_status validate(const cvx_voxinfo* info, const void* tris, const void* table
 	return CVX_OK;
 }
 
+// brick_pairs of the current device's tuning (the default before any call has set it).
+uint32_t current_brick_pairs() {
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) {
+		cudaGetLastError();
+		return Tune().brick_pairs;
+	}
+	std::lock_guard<std::mutex> lk(g_mu);
+	auto it = g_dev.find(dev);
+	return it == g_dev.end() ? Tune().brick_pairs : it->second.tune.brick_pairs;
+}
+
 JobDesc make_job(const cvx_voxinfo& v, const float* tris, uint32_t* table, int morton, int solid) {
 	JobDesc j;
 	std::memset(&j, 0, sizeof(j));
@@ -260,7 +272,7 @@ JobDesc make_job(const cvx_voxinfo& v, const float* tris, uint32_t* table, int m
 	j.flags = (morton ? JOB_MORTON : 0u) | (solid ? JOB_SOLID : 0u);
 	const uint64_t voxels = (uint64_t)v.gridsize[0] * v.gridsize[1] * v.gridsize[2];
 	if (morton ? v.gridsize[0] <= 1024 : voxels <= (1ull << 32)) j.flags |= JOB_NARROW;
-	if (!solid && brick_grid(j.grid)) j.flags |= JOB_BRICKS;
+	if (!solid && brick_grid(j.grid) && current_brick_pairs()) j.flags |= JOB_BRICKS;
 	if (v.n_triangles && needs_plain_loads(tris)) j.flags |= JOB_PLAIN_LOADS;
 	return j;
 }

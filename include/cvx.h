@@ -269,8 +269,8 @@ typedef struct cvx_tuning {
 	uint32_t small_vox;   /* surface: triangles with at most this many bbox voxels stay in one thread */
 	uint32_t small_cols;  /* solid: triangles with at most this many columns stay in one thread */
 	uint32_t brick_pairs; /* surface, grids of 2^29+ voxels: (brick, triangle) pairs per triangle the
-	                       * shared-memory brick rasterizer may use, at most 16; 0 rasterizes every
-	                       * larger triangle row by row with global atomics instead */
+	                       * shared-memory brick rasterizer may use, at most 16; 0 (the default)
+	                       * rasterizes every larger triangle row by row with global atomics instead */
 } cvx_tuning;
 /* Per-device tuning used by subsequent calls (results never depend on it). */
 cvx_status cvx_get_tuning(int device, cvx_tuning* out);
