@@ -311,7 +311,7 @@ def time_cpu_reference(info_bytes, sample, threads):
     t0 = time.perf_counter()
     for morton, solid in MODES:
         if oracle.ref_cpu_available():
-            oracle.ref_cpu_voxelize(info_s, sample, morton=morton, solid=solid)
+            oracle.ref_cpu_voxelize(info_s, sample, morton=morton, solid=solid, quiet=True)
         else:
             oracle.voxelize_omp(info_s, sample, morton=morton, solid=solid, threads=threads)
     return time.perf_counter() - t0

@@ -13,8 +13,10 @@ baseline leg may import this package; the engine in ``cuda_voxelizer_gb300`` nev
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import os
+import sys
 
 import numpy as np
 
@@ -225,7 +227,28 @@ def ref_cpu_available() -> bool:
     return ref_cpu_lib() is not None
 
 
-def ref_cpu_voxelize(info: bytes, tris, morton: bool = False, solid: bool = False) -> np.ndarray:
+@contextlib.contextmanager
+def _stdout_to_devnull():
+    """Send file descriptor 1 to /dev/null for the duration (the reference CPU voxelizer prints
+    "[Info] Using N threads" and "[Perf] CPU voxelization time" on stdout; the shim flushes C stdio
+    before returning, so nothing of it reaches the real stdout afterwards)."""
+    sys.stdout.flush()
+    saved = os.dup(1)
+    null = os.open(os.devnull, os.O_WRONLY)
+    try:
+        os.dup2(null, 1)
+        yield
+    finally:
+        os.dup2(saved, 1)
+        os.close(null)
+        os.close(saved)
+
+
+def ref_cpu_voxelize(info: bytes, tris, morton: bool = False, solid: bool = False,
+                     quiet: bool = False) -> np.ndarray:
+    """The reference's cpu_voxelize_mesh / cpu_voxelize_mesh_solid (src/cpu_voxelizer.cpp:35, :241)
+    on a soup.  ``quiet`` drops the reference's own stdout lines (for callers whose stdout is a
+    machine-read record, like the benchmark's JSON line)."""
     L = ref_cpu_lib()
     if L is None:
         raise RuntimeError("reference CPU build not available on this machine")
@@ -233,7 +256,11 @@ def ref_cpu_voxelize(info: bytes, tris, morton: bool = False, solid: bool = Fals
     ib = ctypes.create_string_buffer(bytes(info), 64)
     table = np.zeros(table_words(info), dtype=np.uint32)
     fn = L.ref_cpu_voxelize_solid if solid else L.ref_cpu_voxelize
-    fn(ctypes.addressof(ib), _ptr(t), _ptr(table), int(morton))
+    if quiet:
+        with _stdout_to_devnull():
+            fn(ctypes.addressof(ib), _ptr(t), _ptr(table), int(morton))
+    else:
+        fn(ctypes.addressof(ib), _ptr(t), _ptr(table), int(morton))
     return table
 
 

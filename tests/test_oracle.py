@@ -116,6 +116,21 @@ def test_oracle_matches_reference_live(seed):
             assert np.array_equal(a, b), (g, morton, solid)
 
 
+@pytest.mark.skipif(not oracle.ref_cpu_available(), reason="reference CPU build not present on this machine")
+def test_reference_cpu_quiet_keeps_stdout_clean(capfd):
+    """The benchmark prints one JSON line on stdout; the reference CPU voxelizer's own "[Info]" and
+    "[Perf]" lines must not reach it when the benchmark times that build."""
+    t = meshgen.torus(0, nu=16, nv=8)
+    info = bytes(cv.make_voxinfo(t, 32))
+    capfd.readouterr()
+    loud = oracle.ref_cpu_voxelize(info, t)
+    assert "[Perf]" in capfd.readouterr().out
+    quiet = oracle.ref_cpu_voxelize(info, t, quiet=True)
+    print("after")
+    assert capfd.readouterr().out == "after\n"
+    assert np.array_equal(loud, quiet)
+
+
 @pytest.mark.parametrize("solid", [False, True])
 @pytest.mark.parametrize("morton", [False, True])
 def test_count_atomics_matches_per_triangle_tables(morton, solid):
