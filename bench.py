@@ -425,7 +425,8 @@ def pc_soup(cv, meshgen, torch):
 
 
 def pc_soup200k(cv, meshgen, torch):
-    """the first 200,000 triangles of that soup at 1024^3 (a small case of the brick kernels)"""
+    """the first 200,000 triangles of that soup at 1024^3 (a small case of surf_rows and of the brick
+    kernels), with the device's current tuning"""
     tris = meshgen.soup(0, n=2_000_000)[:200_000]
     info = cv.make_voxinfo(tris, 1024)
     d = torch.from_numpy(tris.reshape(-1)).cuda()
@@ -437,9 +438,10 @@ def pc_soup200k(cv, meshgen, torch):
     return run
 
 
-def pc_soup200k_rows(cv, meshgen, torch):
-    """the same with the brick rasterizer off (brick_pairs = 0): every larger triangle row by row"""
-    cv.set_tuning(torch.cuda.current_device(), brick_pairs=0)
+def pc_soup200k_bricks(cv, meshgen, torch):
+    """the same with the brick rasterizer on (brick_pairs = 16): the larger triangles binned to 32^3
+    bricks, rasterized in shared memory, one global atomicOr per non-zero brick word"""
+    cv.set_tuning(torch.cuda.current_device(), brick_pairs=16)
     return pc_soup200k(cv, meshgen, torch)
 
 
@@ -497,7 +499,7 @@ def pc_io(cv, meshgen, torch):
 
 
 PROFILE_CASES = {"ico8": pc_ico8, "ico8_plan": pc_ico8_plan, "soup": pc_soup, "soup200k": pc_soup200k,
-                 "soup200k_rows": pc_soup200k_rows,
+                 "soup200k_bricks": pc_soup200k_bricks,
                  "batch": pc_batch, "batch_g512": pc_batch_g512, "io": pc_io}
 
 
