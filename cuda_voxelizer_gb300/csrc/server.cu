@@ -106,8 +106,21 @@ private:
 	std::map<size_t, size_t> free_, live_;
 };
 
+// The requests of one cvx_server_replay call.  They are not entered in the server's id map (a
+// replay of millions of requests would grow it without bound, and each rehash of a large map, made
+// under the server mutex, stopped the worker and the completion callbacks for tens of
+// milliseconds); the worker writes each latency straight into the caller's array at retirement
+// and counts the group down.  Guarded by the server mutex.
+struct ReplayGroup {
+	uint64_t remaining = 0;
+	cvx_status first_err = CVX_OK;
+	std::string first_msg;
+};
+
 struct Request {
 	uint64_t id = 0;
+	ReplayGroup* group = nullptr;  // set for cvx_server_replay's requests
+	double* latency_out = nullptr; // where the worker stores the group request's latency
 	cvx_server_request req{};
 	bool device_tris = false;     // triangles read in place from req.d_triangles
 	bool resident_table = false;  // no host table and kept: the table stays in the arena until released
@@ -131,7 +144,7 @@ struct Window {
 	static constexpr size_t kWindow = size_t(1) << 20;
 	std::vector<double> v;
 	size_t next = 0;
-	Window() { v.reserve(size_t(1) << 16); }
+	Window() { v.reserve(kWindow); }  // grown once here, never under the server mutex
 	void push(double x) {
 		if (v.size() < kWindow) {
 			v.push_back(x);
@@ -350,6 +363,14 @@ struct cvx_server {
 			latencies.push(r->latency_ms);
 			queue_waits.push(std::chrono::duration<double, std::milli>(sl.launch_time - r->arrival).count());
 			completed++;
+			if (ReplayGroup* g = r->group) {
+				*r->latency_out = r->latency_ms;
+				if (r->status != CVX_OK && g->first_err == CVX_OK) {
+					g->first_err = r->status;
+					g->first_msg = r->message;
+				}
+				g->remaining--;
+			}
 		}
 		last_done = sl.finish_time;
 		services.push(std::chrono::duration<double, std::milli>(sl.finish_time - sl.launch_time).count());
@@ -395,10 +416,12 @@ struct cvx_server {
 		}
 	}
 
-	// discard_table: a request without a host table whose table nobody will read (the replay load
-	// generator) is freed at completion instead of staying resident.
+	// group (cvx_server_replay): the request is counted in the group and its latency stored at
+	// *latency_out instead of being entered in the id map; a group request without a host table is
+	// freed at completion instead of staying resident (nobody will read it).
 	cvx_status submit(const cvx_server_request* q, Clock::time_point arrival, uint64_t* out_id,
-	                  bool discard_table = false) {
+	                  ReplayGroup* group = nullptr, double* latency_out = nullptr) {
+		const bool discard_table = group != nullptr;
 		if (!q || !out_id) {
 			cvx::set_message("cvx_server_submit: null argument");
 			return CVX_ERR_INVALID_VALUE;
@@ -452,7 +475,13 @@ struct cvx_server {
 			if (!have_first || arrival < first_arrival) first_arrival = arrival;
 			have_first = true;
 			pending.push_back(r);
-			live[r->id] = r;
+			if (group) {
+				r->group = group;
+				r->latency_out = latency_out;
+				group->remaining++;
+			} else {
+				live[r->id] = r;
+			}
 			*out_id = r->id;
 		}
 		cv_work.notify_one();
@@ -662,12 +691,12 @@ cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint
 			return CVX_ERR_INVALID_VALUE;
 		}
 	}
-	std::vector<uint64_t> ids(n);
 	std::vector<double> late(n);
+	ReplayGroup group;
 	const Clock::time_point t0 = Clock::now();
-	cvx_status first_err = CVX_OK;
-	std::string first_msg;
-	for (uint32_t i = 0; i < n; i++) {
+	cvx_status st = CVX_OK;
+	uint32_t submitted = 0;
+	for (uint32_t i = 0; i < n && st == CVX_OK; i++) {
 		const auto due = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
 		// sleep to 50 us before the arrival, then spin: a generator that spins longer keeps a whole
 		// core busy at high rates and competes with the server's own threads
@@ -676,25 +705,24 @@ cvx_status cvx_server_replay(cvx_server* s, const cvx_server_request* reqs, uint
 		while ((now = Clock::now()) < due) {
 		}
 		late[i] = std::chrono::duration<double, std::milli>(now - due).count();
-		const cvx_status st = s->submit(&reqs[i], due, &ids[i], reqs[i].h_table == nullptr);
-		if (st != CVX_OK) {
-			for (uint32_t k = 0; k < i; k++) s->wait(ids[k], -1.0, nullptr);
-			return st;
-		}
+		uint64_t id = 0;
+		st = s->submit(&reqs[i], due, &id, &group, &latency_ms[i]);
+		if (st == CVX_OK) submitted++;
 	}
-	{
+	const std::string submit_msg = st == CVX_OK ? std::string() : cvx_last_error_message();
+	// Generator lateness into the statistics, a slice at a time so the worker is not held up.
+	for (uint32_t i = 0; i < submitted; i += 4096) {
 		std::lock_guard<std::mutex> lk(s->mu);
-		for (double x : late) s->replay_late.push(x);
+		for (uint32_t k = i; k < std::min(submitted, i + 4096); k++) s->replay_late.push(late[k]);
 	}
-	for (uint32_t i = 0; i < n; i++) {
-		const cvx_status st = s->wait(ids[i], -1.0, &latency_ms[i]);
-		if (st != CVX_OK && first_err == CVX_OK) {
-			first_err = st;
-			first_msg = cvx_last_error_message();
-		}
+	std::unique_lock<std::mutex> lk(s->mu);
+	s->cv_done.wait(lk, [&] { return group.remaining == 0; });  // every submitted request retired
+	if (st != CVX_OK) {
+		cvx::set_message(submit_msg);
+		return st;
 	}
-	if (first_err != CVX_OK) cvx::set_message(first_msg);
-	return first_err;
+	if (group.first_err != CVX_OK) cvx::set_message(group.first_msg);
+	return group.first_err;
 }
 
 cvx_status cvx_server_destroy(cvx_server* s) {
