@@ -225,6 +225,23 @@ uint64_t words_of(const cvx_voxinfo& v) {
 	return (bits + 31) / 32;
 }
 
+// For each table range (first word, word count): does it overlap another job's range?  Jobs that
+// share table words accumulate into them (OR / XOR, as repeated reference calls would), so the
+// engine may neither overwrite such a table nor run those jobs on concurrent lanes.
+std::vector<char> overlapping_tables(const std::vector<std::pair<uint32_t*, uint64_t>>& t) {
+	std::vector<char> shared(t.size(), 0);
+	std::vector<size_t> order(t.size());
+	for (size_t i = 0; i < order.size(); i++) order[i] = i;
+	std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return t[a].first < t[b].first; });
+	size_t reach = 0;  // the job whose range ends last among those seen
+	for (size_t k = 0; k < order.size(); k++) {
+		const size_t i = order[k];
+		if (k > 0 && t[i].first < t[reach].first + t[reach].second) shared[i] = shared[reach] = 1;
+		if (k == 0 || t[i].first + t[i].second > t[reach].first + t[reach].second) reach = i;
+	}
+	return shared;
+}
+
 cvx_status validate(const cvx_voxinfo* info, const void* tris, const void* table, int morton) {
 	if (!info) return fail(CVX_ERR_INVALID_VALUE, "info is null");
 	for (int i = 0; i < 3; i++) {
@@ -541,12 +558,12 @@ cvx_status cvx::batch_scratch_bytes(const cvx_job* jobs, uint32_t n_jobs, size_t
 
 cvx_status cvx::run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* const* flips, void* d_rec,
                              size_t rec_bytes, void* h_staging, size_t staging_bytes, cudaStream_t s,
-                             bool tables_zeroed) {
+                             bool overwrite_solid) {
 	std::vector<JobDesc> surf, solid;
 	cvx_status st = collect_jobs(jobs, n_jobs, flips, surf, solid);
 	if (st != CVX_OK) return st;
-	if (tables_zeroed)
-		for (JobDesc& j : solid) j.flags |= JOB_TABLE_ZERO;
+	if (overwrite_solid)
+		for (JobDesc& j : solid) j.flags |= JOB_TABLE_OVERWRITE;
 	if (surf.empty() && solid.empty()) return CVX_OK;
 	if (!solid.empty() && !flips) return fail(CVX_ERR_INVALID_VALUE, "solid jobs need flip tables");
 	const uint64_t cap = queue_cap(surf, solid);
@@ -851,9 +868,24 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		cvx_status st = validate(&jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton);
 		if (st != CVX_OK) return fail(st, "job %u: %s", i, g_msg.c_str());
 		tables.push_back({jobs[i].d_table, words_of(jobs[i].info)});
-		if (jobs[i].info.n_triangles == 0) continue;
+	}
+	// With CVX_PLAN_CLEAR_TABLES every table starts from zero.  A solid job with its own table
+	// overwrites it (no clear needed); the others' tables are zeroed by their lane before its kernels
+	// (or all at the start when jobs share tables: such a plan runs its lanes one after another).
+	const std::vector<char> shared = overlapping_tables(tables);
+	bool any_shared = false;
+	for (char c : shared) any_shared = any_shared || c;
+	const bool clear = (flags & CVX_PLAN_CLEAR_TABLES) != 0;
+	const bool lane_clears = clear && !any_shared;  // surface tables zeroed in their own lane
+	std::vector<std::pair<uint32_t*, uint64_t>> pre_clears;  // zeroed before the lanes fork
+	for (uint32_t i = 0; i < n_jobs; i++) {
+		if (jobs[i].info.n_triangles == 0) {
+			if (clear) pre_clears.push_back(tables[i]);  // complete once cleared
+			continue;
+		}
 		JobDesc j = make_job(jobs[i].info, jobs[i].d_triangles, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
-		if (flags & CVX_PLAN_CLEAR_TABLES) j.flags |= JOB_TABLE_ZERO;  // the graph zeroes it first
+		if (clear && jobs[i].solid && !shared[i]) j.flags |= JOB_TABLE_OVERWRITE;
+		else if (clear && !(lane_clears && !jobs[i].solid)) pre_clears.push_back(tables[i]);
 		(jobs[i].solid ? solid : surf).push_back(j);
 	}
 	DevState dev;
@@ -872,6 +904,8 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		uint64_t cap = 1;
 		uint32_t bricks = 0;         // largest brick count of the lane's groups
 		size_t job_off = 0;          // first JobDesc slot of the lane in the job area
+		size_t clear_off = 0;        // the lane's tables to zero: ranges [clear_off, clear_off + clear_n)
+		uint32_t clear_n = 0, clear_chunks = 0;
 		cudaStream_t stream = nullptr;
 		cudaEvent_t done = nullptr;
 	};
@@ -941,12 +975,24 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		}
 		p->recs.push_back(rec);
 	}
+	// The clear list: the tables zeroed before the fork, then each surface lane's own tables (each
+	// segment numbers its chunks from 0: one clear_ranges launch per segment).
 	std::vector<ClearRange> clears;
 	uint32_t clear_total = 0;
-	if (flags & CVX_PLAN_CLEAR_TABLES) {
-		for (auto& t : tables) {
+	if (clear) {
+		for (auto& t : pre_clears) {
 			clears.push_back(ClearRange{t.first, t.second, clear_total, 0u});
 			clear_total += clear_chunks(t.second);
+		}
+		for (Lane& l : lanes) {
+			if (l.solid || !lane_clears) continue;
+			l.clear_off = clears.size();
+			for (const JobDesc& j : l.jobs) {
+				const uint64_t words = ((uint64_t)j.grid[0] * j.grid[1] * j.grid[2] + 31) / 32;
+				clears.push_back(ClearRange{j.table, words, l.clear_chunks, 0u});
+				l.clear_chunks += clear_chunks(words);
+			}
+			l.clear_n = (uint32_t)(clears.size() - l.clear_off);
 		}
 		if (!clears.empty()) {
 			if (cudaMalloc((void**)&p->clears, clears.size() * sizeof(ClearRange)) != cudaSuccess) {
@@ -963,7 +1009,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 	cudaEvent_t fork_ev;
 	if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "stream"));
 	cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming);
-	const bool fork = lanes.size() > 1;
+	const bool fork = lanes.size() > 1 && !any_shared;  // jobs sharing a table run one after another
 	cvx_status cst = CVX_OK;
 	for (Lane& l : lanes) {
 		l.stream = cs;
@@ -991,7 +1037,7 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		drop_streams();
 		return bail(cuda_fail(cudaGetLastError(), "begin capture"));
 	}
-	if (!clears.empty() && launch_clear(p->clears, (uint32_t)clears.size(), clear_total, cs) != cudaSuccess)
+	if (!pre_clears.empty() && launch_clear(p->clears, (uint32_t)pre_clears.size(), clear_total, cs) != cudaSuccess)
 		cst = cuda_fail(cudaGetLastError(), "table clear");
 	if (cst == CVX_OK && fork && cudaEventRecord(fork_ev, cs) != cudaSuccess) cst = cuda_fail(cudaGetLastError(), "capture fork");
 	// Launch exactly like Runner::run, but with the job arrays already resident.
@@ -999,7 +1045,8 @@ cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags,
 		Lane& l = lanes[li];
 		void* rec = p->recs[li];
 		if ((fork && cudaStreamWaitEvent(l.stream, fork_ev, 0) != cudaSuccess) ||
-		    cudaMemsetAsync(rec, 0, rec_layout(l.cap, 0, l.bricks).big, l.stream) != cudaSuccess) {
+		    cudaMemsetAsync(rec, 0, rec_layout(l.cap, 0, l.bricks).big, l.stream) != cudaSuccess ||
+		    (l.clear_n && launch_clear(p->clears + l.clear_off, l.clear_n, l.clear_chunks, l.stream) != cudaSuccess)) {
 			cst = cuda_fail(cudaGetLastError(), "capture lane");
 			break;
 		}
@@ -1146,12 +1193,18 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 			for (size_t k = 0; k < idx.size(); k++) flips[idx[k]] = full[k].flips;
 		}
 	}
+	// Every launch rewrites every table: a solid job with a table of its own overwrites it (its
+	// resolve stores every word); the other tables are zeroed at the start of the launch.
+	std::vector<std::pair<uint32_t*, uint64_t>> ranges;
+	for (uint32_t i = 0; i < n_jobs; i++) ranges.push_back({jobs[i].d_table, words_of(jobs[i].info)});
+	const std::vector<char> shared = overlapping_tables(ranges);
+	auto overwrites = [&](uint32_t i) { return jobs[i].solid && up_of[i] >= 0 && !shared[i]; };
 	auto job_of = [&](uint32_t i, uint64_t b0, uint64_t b1) {
 		cvx_voxinfo v = jobs[i].info;
 		v.n_triangles = b1 - b0;
 		JobDesc j = make_job(v, jobs[i].d_triangles + 9 * b0, jobs[i].d_table, jobs[i].morton, jobs[i].solid);
 		j.flips = flips[i];
-		j.flags |= JOB_TABLE_ZERO;  // the plan zeroes every table first
+		if (overwrites(i)) j.flags |= JOB_TABLE_OVERWRITE;
 		return j;
 	};
 	// The compute stream's steps.  Jobs without triangles are complete once cleared.
@@ -1311,7 +1364,8 @@ cvx_status cvx_plan_create_host(const cvx_host_job* jobs, uint32_t n_jobs, uint3
 			ck(cudaEventRecord(landed[u][c], cp), "capture upload");
 		}
 	ck(cudaEventRecord(copied, cp), "capture upload");
-	for (uint32_t i = 0; i < n_jobs; i++) ck(cudaMemsetAsync(jobs[i].d_table, 0, words_of(jobs[i].info) * 4, cs), "capture clear");
+	for (uint32_t i = 0; i < n_jobs; i++)
+		if (!overwrites(i)) ck(cudaMemsetAsync(jobs[i].d_table, 0, words_of(jobs[i].info) * 4, cs), "capture clear");
 	ck(cudaMemsetAsync(rec, 0, rec_layout(cap, 0, bricks).big, cs), "capture clear");
 	for (const HostStep& st : steps) {
 		if (cst != CVX_OK) break;

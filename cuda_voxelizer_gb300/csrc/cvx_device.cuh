@@ -69,15 +69,16 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 // JOB_NARROW: every voxel index of the job fits 32 bits (linear: gx*gy*gz <= 2^32; Morton: a cubic
 // grid of at most 1024), so the surface writes compute indices and Morton codes in 32-bit
 // arithmetic.  Set by the host; a hint only (the 64-bit path gives the same words).
-// JOB_TABLE_ZERO: the engine zeroed the job's table earlier in the same launch sequence (plans that
-// clear their tables, host plans, server batches), so the solid passes store their words instead of
-// XOR-ing them into the table (same result, no read) and skip words that resolve to zero.
+// JOB_TABLE_OVERWRITE (solid jobs): the engine owns the table's content in this launch sequence
+// (plans that clear their tables, host plans, server batches): the resolve passes store every word
+// of the table, zeros included, instead of XOR-ing into it.  The table need not be zeroed first:
+// the result equals XOR-ing into a zeroed table, with one write per word and no read.
 // JOB_PLAIN_LOADS: the job's triangles are not plain device memory (managed, host-registered or
 // system memory -- the reference's main() passes cudaMallocManaged buffers): the classify kernels
 // read them with ordinary loads instead of bulk copies.
 // JOB_BRICKS: a surface job whose queued (larger) triangles are rasterized brick by brick in shared
 // memory (bricks.cu) instead of by per-row global atomics.
-enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u, JOB_TABLE_ZERO = 8u, JOB_PLAIN_LOADS = 16u,
+enum : uint32_t { JOB_MORTON = 1u, JOB_SOLID = 2u, JOB_NARROW = 4u, JOB_TABLE_OVERWRITE = 8u, JOB_PLAIN_LOADS = 16u,
                   JOB_BRICKS = 32u };
 
 // One mesh voxelization.  Plain data, uploaded as an array for batches or passed by value for a
@@ -91,7 +92,7 @@ struct JobDesc {
 	float unit[3];
 	float inv_unit[3];     // 1.0f / unit, correctly rounded (host); only used for the exactly checked div_trunc
 	uint32_t grid[3];
-	uint32_t flags;        // JOB_MORTON | JOB_SOLID | JOB_NARROW | JOB_TABLE_ZERO
+	uint32_t flags;        // JOB_MORTON | JOB_SOLID | JOB_NARROW | JOB_TABLE_OVERWRITE | ...
 	uint32_t tile_begin;   // first triangle tile of this job in the launch's tile space
 	uint32_t unit_begin;   // solid: first resolve unit of this job in the launch's unit space
 	uint64_t mword_begin;  // solid Morton, g < 32: first Morton word in the launch's word space

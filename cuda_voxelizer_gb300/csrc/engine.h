@@ -135,10 +135,11 @@ cvx_status noalloc_error(int dev, unsigned* err);
 // batch_scratch_bytes gives the device record bytes (256-byte aligned) and the pinned host staging
 // bytes that run_batch_on needs for `jobs`.  run_batch_on takes one flip table per job in `flips`
 // (read for solid jobs only: table-sized, zero on entry, zero again afterwards); the staging buffer
-// must stay untouched until the stream has passed this call.  tables_zeroed: the caller zeroed every
-// job's table on stream s before this call (the solid passes then store instead of XOR-ing).
+// must stay untouched until the stream has passed this call.  overwrite_solid: the solid jobs' tables
+// belong to the caller's launch alone (no other job writes them): their resolve stores every word,
+// so they need not be zeroed (JOB_TABLE_OVERWRITE); the surface jobs' tables must be zero.
 cvx_status batch_scratch_bytes(const cvx_job* jobs, uint32_t n_jobs, size_t* rec_bytes, size_t* staging_bytes);
 cvx_status run_batch_on(const cvx_job* jobs, uint32_t n_jobs, uint32_t* const* flips, void* d_rec, size_t rec_bytes,
-                        void* h_staging, size_t staging_bytes, cudaStream_t s, bool tables_zeroed = false);
+                        void* h_staging, size_t staging_bytes, cudaStream_t s, bool overwrite_solid = false);
 
 }  // namespace cvx

@@ -316,8 +316,10 @@ struct cvx_server {
 				ok = cuda_ok(cudaMemcpyAsync(r->d_tris, r->req.h_triangles, r->tri_bytes, cudaMemcpyHostToDevice, st),
 				             "cudaMemcpyAsync(triangles)");
 			const uint64_t words = r->table_bytes / 4;
-			sl.h_clears[n_ranges++] = cvx::ClearRange{static_cast<uint32_t*>(r->d_table), words, chunks, 0u};
-			chunks += cvx::clear_chunks(words);
+			if (!r->req.solid || r->req.info.n_triangles == 0) {  // solid tables are overwritten by their resolve
+				sl.h_clears[n_ranges++] = cvx::ClearRange{static_cast<uint32_t*>(r->d_table), words, chunks, 0u};
+				chunks += cvx::clear_chunks(words);
+			}
 			if (r->flip_bytes) {
 				sl.h_clears[n_ranges++] = cvx::ClearRange{static_cast<uint32_t*>(r->d_flips), words, chunks, 0u};
 				chunks += cvx::clear_chunks(words);

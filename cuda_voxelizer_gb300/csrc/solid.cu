@@ -16,8 +16,8 @@
 //                       CTA, the other triangles queued.
 //   solid_cols          persistent; each warp takes items of up to kColsPerItem columns.
 //   solid_resolve       linear jobs: one thread per row run (whole rows; 16-byte words where rows
-//                       are aligned): prefix XOR along x, XORed into the linear table (stored, for
-//                       JOB_TABLE_ZERO jobs), flip table cleared.
+//                       are aligned): prefix XOR along x, XORed into the linear table (every word
+//                       stored, for JOB_TABLE_OVERWRITE jobs), flip table cleared.
 //   solid_morton_slab   Morton jobs with 32 <= g <= 1024: a CTA resolves a 16 x 16-row slab in
 //                       shared memory and writes it as 16^3 Morton blocks (128 contiguous words).
 //   solid_morton_brick  Morton jobs with g > 1024: groups of x-adjacent 32^3 bricks.
@@ -485,19 +485,18 @@ __device__ __forceinline__ uint32_t resolve_word(uint32_t t, uint32_t& carry) {
 // Linear jobs: table ^= resolved, toggles cleared.  Morton jobs: toggles replaced by the resolved
 // bits for solid_morton_* to gather.
 // XOR a resolved word into the table (the reference's semantics: the caller's table is XORed), or
-// store it when the engine zeroed the table itself (JOB_TABLE_ZERO): same words, no read.
-__device__ __forceinline__ void xor_out(uint32_t* dest, uint64_t w, uint32_t v, bool zero) {
-	if (!v) return;
-	if (zero) dest[w] = v;
-	else dest[w] ^= v;
+// store it, zero or not, when the engine owns the table's content (JOB_TABLE_OVERWRITE).
+__device__ __forceinline__ void xor_out(uint32_t* dest, uint64_t w, uint32_t v, bool overwrite) {
+	if (overwrite) dest[w] = v;
+	else if (v) dest[w] ^= v;
 }
 
 __device__ __forceinline__ void resolve_store(uint32_t* flips, uint32_t* dest, uint64_t w, uint32_t t, uint32_t res,
-                                              bool morton, bool zero) {
+                                              bool morton, bool overwrite) {
 	if (morton) {
 		if (res != t) flips[w] = res;
 	} else {
-		xor_out(dest, w, res, zero);
+		xor_out(dest, w, res, overwrite);
 		if (t) flips[w] = 0u;
 	}
 }
@@ -515,7 +514,7 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 	const uint64_t gx = J.grid[0];
 	const uint64_t rows = (uint64_t)J.grid[1] * J.grid[2];
 	const bool morton = (J.flags & JOB_MORTON) != 0;
-	const bool zero = (J.flags & JOB_TABLE_ZERO) != 0;
+	const bool overwrite = (J.flags & JOB_TABLE_OVERWRITE) != 0 && !morton;  // Morton words: written below
 	uint32_t* flips = J.flips;
 	uint32_t* dest = J.table;
 	const uint64_t u = unit_id - J.unit_begin;
@@ -528,13 +527,16 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 		if (vec) {
 			for (uint32_t i = 0; i < wpr; i += 4) {
 				const uint4 t = *reinterpret_cast<const uint4*>(flips + w0 + i);
-				if ((t.x | t.y | t.z | t.w) == 0u && carry == 0u) continue;  // outside the solid
+				if ((t.x | t.y | t.z | t.w) == 0u && carry == 0u) {  // outside the solid
+					if (overwrite) *reinterpret_cast<uint4*>(dest + w0 + i) = make_uint4(0u, 0u, 0u, 0u);
+					continue;
+				}
 				const uint32_t r0 = resolve_word(t.x, carry), r1 = resolve_word(t.y, carry);
 				const uint32_t r2 = resolve_word(t.z, carry), r3 = resolve_word(t.w, carry);
 				if (morton) {
 					*reinterpret_cast<uint4*>(flips + w0 + i) = make_uint4(r0, r1, r2, r3);
-				} else if (zero) {
-					if (r0 | r1 | r2 | r3) *reinterpret_cast<uint4*>(dest + w0 + i) = make_uint4(r0, r1, r2, r3);
+				} else if (overwrite) {
+					*reinterpret_cast<uint4*>(dest + w0 + i) = make_uint4(r0, r1, r2, r3);
 					if (t.x | t.y | t.z | t.w) *reinterpret_cast<uint4*>(flips + w0 + i) = make_uint4(0u, 0u, 0u, 0u);
 				} else {
 					uint4 d = *reinterpret_cast<const uint4*>(dest + w0 + i);
@@ -546,8 +548,11 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 		} else {
 			for (uint32_t i = 0; i < wpr; i++) {
 				const uint32_t t = flips[w0 + i];
-				if (t == 0u && carry == 0u) continue;
-				resolve_store(flips, dest, w0 + i, t, resolve_word(t, carry), morton, zero);
+				if (t == 0u && carry == 0u) {
+					if (overwrite) dest[w0 + i] = 0u;
+					continue;
+				}
+				resolve_store(flips, dest, w0 + i, t, resolve_word(t, carry), morton, overwrite);
 			}
 		}
 	} else {
@@ -572,7 +577,7 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 				carry ^= (t >> (31 - k)) & 1u;
 				res |= carry << (31 - k);
 			}
-			resolve_store(flips, dest, w, t, res, morton, zero);
+			resolve_store(flips, dest, w, t, res, morton, overwrite);
 		}
 	}
 }
@@ -635,7 +640,7 @@ __global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant_
 					const uint32_t nib = (row >> (28u - 4u * X)) & 0xFu;
 					out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 				}
-			xor_out(dest, m, out, (J.flags & JOB_TABLE_ZERO) != 0);
+			xor_out(dest, m, out, (J.flags & JOB_TABLE_OVERWRITE) != 0);
 		}
 	}
 }
@@ -701,7 +706,7 @@ __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__
 				const uint32_t nib = (rw >> (28u - xoff)) & 0xFu;
 				out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 			}
-		xor_out(J.table, (blk << 7) + m, out, (J.flags & JOB_TABLE_ZERO) != 0);
+		xor_out(J.table, (blk << 7) + m, out, (J.flags & JOB_TABLE_OVERWRITE) != 0);
 	}
 }
 
@@ -725,7 +730,7 @@ __global__ void __launch_bounds__(256) solid_morton_small(const __grid_constant_
 		const uint64_t lin = x + g * (y + g * z);
 		out |= ((flips[lin >> 5] >> (31u - (uint32_t)(lin & 31u))) & 1u) << (31u - i);
 	}
-	xor_out(J.table, m, out, (J.flags & JOB_TABLE_ZERO) != 0);
+	xor_out(J.table, m, out, (J.flags & JOB_TABLE_OVERWRITE) != 0);
 }
 
 // Morton jobs with g < 32: clear the resolved flip table, one thread per resolve unit (the larger

@@ -138,7 +138,11 @@ cvx_status cvx_voxelize_batch(const cvx_job* jobs, uint32_t n_jobs, cvx_stream_t
 
 /* A batch prepared once and replayed as one CUDA graph launch. */
 typedef struct cvx_plan cvx_plan;
-#define CVX_PLAN_CLEAR_TABLES 1u /* the graph zeroes every job's table before voxelizing */
+/* CVX_PLAN_CLEAR_TABLES: every launch gives each table exactly what voxelizing into a zeroed table
+ * gives, whatever the table held (surface tables are zeroed inside the graph, solid tables are
+ * written word by word).  Jobs whose tables share words accumulate into them (OR, then XOR).
+ * Without the flag, jobs OR / XOR into their tables like the per-call functions. */
+#define CVX_PLAN_CLEAR_TABLES 1u
 cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out);
 cvx_status cvx_plan_launch(cvx_plan* plan, cvx_stream_t stream);
 cvx_status cvx_plan_destroy(cvx_plan* plan);

@@ -407,7 +407,12 @@ def test_batch_equals_single_calls():
 
 
 def test_plan_equals_single_calls_and_replays():
+    """A clearing plan starts every table from zero whatever it held: surface tables are zeroed by
+    their lane, solid tables are overwritten word by word by their resolve (the guard words after
+    each table must stay zero)."""
     jobs = _mixed_jobs()
+    for j in jobs:
+        j.table[:cv.table_words(j.info)] = 0x5A5A5A5A  # dirty tables
     plan = cv.Plan(jobs, clear_tables=True)
     for _ in range(3):
         plan.launch()
@@ -416,6 +421,33 @@ def test_plan_equals_single_calls_and_replays():
         single = run_engine(j.info, j.triangles, j.morton, j.solid)
         torch.cuda.synchronize()
         assert torch.equal(single, j.table)
+    plan.close()
+
+
+def test_plan_jobs_sharing_a_table_accumulate():
+    """Jobs whose tables share words accumulate into them as repeated reference calls would: a
+    clearing plan zeroes the shared table once, the surface job ORs, the solid job XORs (the plan
+    runs such jobs one after another instead of on concurrent lanes)."""
+    t1, t2 = meshgen.torus(30), meshgen.icosphere(31, 5)
+    info1, info2 = info_of(t1, 64), info_of(t2, 64)
+    d1, d2 = torch.from_numpy(t1.reshape(-1)).cuda(), torch.from_numpy(t2.reshape(-1)).cuda()
+    W = cv.table_words(info1)
+    shared = torch.full((W + GUARD,), 0x5A5A5A5A, dtype=torch.int32, device="cuda")
+    shared[W:] = 0
+    other = torch.full((W + GUARD,), 0x5A5A5A5A, dtype=torch.int32, device="cuda")
+    other[W:] = 0
+    jobs = [cv.Job(info1, d1, shared, False, False), cv.Job(info2, d2, shared, False, True),
+            cv.Job(info2, d2, other, False, True)]
+    plan = cv.Plan(jobs, clear_tables=True)
+    for _ in range(2):
+        plan.launch()
+    torch.cuda.synchronize()
+    cv.device_status()
+    surf = run_engine(info1, d1, False, False)
+    solid = run_engine(info2, d2, False, True)
+    torch.cuda.synchronize()
+    assert torch.equal(shared, surf ^ solid)
+    assert torch.equal(other, solid)
     plan.close()
 
 
