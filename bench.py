@@ -480,6 +480,17 @@ def pc_batch_g512(cv, meshgen, torch):
     return run
 
 
+def pc_batch_g512_solid(cv, meshgen, torch):
+    """the solid meshes of that mix gridded at 512^3, as one batch"""
+    jobs = _pc_mix_jobs(cv, meshgen, torch, lambda spec: spec.solid and spec.gridsize == 512)
+
+    def run():
+        for j in jobs:
+            j.table.zero_()
+        cv.voxelize_batch(jobs)
+    return run
+
+
 def pc_io(cv, meshgen, torch):
     """a random 1024^3 table transcoded linear -> Morton -> linear, then the 512^3 solid icosphere's
     binvox payload and voxel list"""
@@ -500,7 +511,8 @@ def pc_io(cv, meshgen, torch):
 
 PROFILE_CASES = {"ico8": pc_ico8, "ico8_plan": pc_ico8_plan, "soup": pc_soup, "soup200k": pc_soup200k,
                  "soup200k_bricks": pc_soup200k_bricks,
-                 "batch": pc_batch, "batch_g512": pc_batch_g512, "io": pc_io}
+                 "batch": pc_batch, "batch_g512": pc_batch_g512, "batch_g512_solid": pc_batch_g512_solid,
+                 "io": pc_io}
 
 
 def run_profile_case(name, reps):

@@ -135,8 +135,6 @@ __device__ __forceinline__ void queue_for_rows(const LaunchDesc& L, uint32_t job
 
 template <class P>
 __global__ void __launch_bounds__(kBinThreads) brick_bin(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // the brick queue is the classify kernel's output
-	pdl_trigger();
 	const uint32_t lane = threadIdx.x & 31u;
 	Counters* C = L.scr.ctr;
 	__shared__ unsigned s_n;
@@ -193,8 +191,6 @@ __global__ void __launch_bounds__(kBinThreads) brick_bin(const __grid_constant__
 // Exclusive prefix sums over the launch's bricks: pair offsets and raster work units.  The counts
 // are cleared for the next launch sequence.
 __global__ void __launch_bounds__(kScanThreads) brick_scan(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // the pair counts are brick_bin's output
-	pdl_trigger();
 	__shared__ uint32_t s_c[kScanThreads / 32], s_u[kScanThreads / 32];
 	const uint32_t n = L.n_bricks, lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 	const uint32_t per = (n + kScanThreads - 1) / kScanThreads;
@@ -244,8 +240,6 @@ __global__ void __launch_bounds__(kScanThreads) brick_scan(const __grid_constant
 // The binned triangles' pairs into their bricks' slot ranges (same candidates and tests as brick_bin,
 // from the cached setup).
 __global__ void __launch_bounds__(kBinThreads) brick_fill(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // offsets from brick_scan
-	pdl_trigger();
 	const uint32_t lane = threadIdx.x & 31u;
 	Counters* C = L.scr.ctr;
 	__shared__ unsigned s_n;
@@ -382,8 +376,6 @@ __device__ __forceinline__ void raster_pair(const SurfTri& S, const float* v0, c
 template <class P>
 __global__ void __launch_bounds__(kRowsThreads, 3) brick_raster(const __grid_constant__ LaunchDesc L) {
 	__shared__ __align__(16) uint32_t s_bricks[kRasterWarps][kBrickWords];
-	pdl_wait();  // the sorted pairs are brick_fill's output
-	pdl_trigger();
 	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 	uint32_t* s = s_bricks[warp];
 	Counters* C = L.scr.ctr;
@@ -460,16 +452,16 @@ __global__ void __launch_bounds__(kRowsThreads, 3) brick_raster(const __grid_con
 
 template <class P>
 static cudaError_t launch_bricks_t(const LaunchDesc& L, int grid, int raster_grid, cudaStream_t s, const Prof* prof) {
-	cudaError_t e = launch_after(brick_bin<P>, (unsigned)grid, kBinThreads, 0, s, L);
+	cudaError_t e = launch_k(brick_bin<P>, (unsigned)grid, kBinThreads, 0, s, L);
 	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("brick_bin", s);
-	e = launch_after(brick_scan, 1u, kScanThreads, 0, s, L);
+	e = launch_k(brick_scan, 1u, kScanThreads, 0, s, L);
 	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("brick_scan", s);
-	e = launch_after(brick_fill, (unsigned)grid, kBinThreads, 0, s, L);
+	e = launch_k(brick_fill, (unsigned)grid, kBinThreads, 0, s, L);
 	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("brick_fill", s);
-	e = launch_after(brick_raster<P>, (unsigned)raster_grid, kRowsThreads, 0, s, L);
+	e = launch_k(brick_raster<P>, (unsigned)raster_grid, kRowsThreads, 0, s, L);
 	if (e != cudaSuccess) return e;
 	if (prof) (*prof)("brick_raster", s);
 	return cudaGetLastError();

@@ -361,14 +361,6 @@ __device__ __forceinline__ uint32_t job_search(const LaunchDesc& L, uint64_t idx
 	return lo;
 }
 
-// Programmatic dependent launch.  A kernel launched with launch_after (engine.h) may be scheduled
-// while its predecessor on the stream is still draining; it calls pdl_wait() before it reads
-// anything the predecessor wrote (the wait returns once the predecessor has completed and its
-// writes are visible, and at once for a kernel launched without the attribute).  pdl_trigger()
-// lets the successor be scheduled as soon as every CTA of this grid has started.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
 __device__ __forceinline__ void set_error(const LaunchDesc& L, unsigned code) {
 	atomicCAS(&L.scr.ctr->error, 0u, code);
 }

@@ -9,8 +9,7 @@
 // XORs the resolved bits into the caller's table (or scatters them into Morton order).  The XOR of
 // any set of [0, xmax] ranges is exactly what this produces.
 //
-// Kernels, in launch order (each after the first launched with launch_after, waiting on its
-// predecessor with pdl_wait):
+// Kernels, in launch order:
 //   solid_classify      one CTA per 256-triangle tile (TMA bulk staging as in surface.cu); the
 //                       columns of triangles with at most `small_cols` columns are dealt over the
 //                       CTA, the other triangles queued.
@@ -280,7 +279,6 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 	__shared__ uint32_t s_items[kTile * kSmallCols];  // (triangle | dy << 8 | dz << 16) per column
 	__shared__ uint32_t s_warp[kTile / 32];
 	__shared__ __align__(8) uint64_t s_bar;
-	pdl_trigger();  // solid_cols may be scheduled as this grid's last wave runs
 	const uint32_t tile = blockIdx.x;
 	const uint32_t j = job_of_tile(L, tile);
 	const JobDesc& J = job_at(L, j);
@@ -385,8 +383,6 @@ __global__ void __launch_bounds__(kTile) solid_classify(const __grid_constant__ 
 
 template <class P>
 __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // reads what the previous kernel of the sequence wrote
-	pdl_trigger();
 	const uint32_t lane = threadIdx.x & 31u;
 	Counters* C = L.scr.ctr;
 	__shared__ unsigned long long s_bigc;  // read once per CTA (see surf_rows)
@@ -505,8 +501,6 @@ __device__ __forceinline__ void resolve_store(uint32_t* flips, uint32_t* dest, u
 // loads when the row and both tables are 16-byte aligned).  Other gx: the shortest run of rows
 // that starts and ends on word boundaries, walked bit by bit (odd grid sizes only).
 __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // reads what the previous kernel of the sequence wrote
-	pdl_trigger();
 	const uint32_t unit_id = blockIdx.x * blockDim.x + threadIdx.x;
 	if (unit_id >= L.n_units) return;
 	const uint32_t j = job_search(L, unit_id, [](const JobDesc& d) { return (uint64_t)d.unit_begin; });
@@ -590,8 +584,6 @@ __global__ void __launch_bounds__(256) solid_resolve(const __grid_constant__ Lau
 // their only reader), then each Morton word is assembled from eight 4-bit row nibbles and XORed into
 // the table with coalesced accesses.
 __global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // reads what the previous kernel of the sequence wrote
-	pdl_trigger();
 	__shared__ __align__(16) uint32_t s_rows[32 * 32 * 4];  // [z][y][W] words of x-bits
 	const uint64_t group = blockIdx.x;
 	const uint32_t j = job_search(L, group, [](const JobDesc& d) { return d.mbrick_begin; });
@@ -652,8 +644,6 @@ __global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant_
 // resolves one whole row (prefix XOR along x); then every 16^3 block along x -- 128 consecutive
 // Morton words -- is gathered from 4-bit row nibbles and XORed into the table.
 __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // reads what the previous kernel of the sequence wrote
-	pdl_trigger();
 	extern __shared__ __align__(16) uint32_t s_slab[];  // row zi*16 + yi at slab_row(row, stride)
 	const uint64_t slab = blockIdx.x;
 	const uint32_t j = job_search(L, slab, [](const JobDesc& d) { return d.mslab_begin; });
@@ -712,8 +702,6 @@ __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__
 
 // Morton jobs with g < 32: one Morton word per thread, 32 codes decoded one by one.
 __global__ void __launch_bounds__(256) solid_morton_small(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // reads what the previous kernel of the sequence wrote
-	pdl_trigger();
 	const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
 	if (idx >= L.n_mwords) return;
 	const uint32_t j = job_search(L, idx, [](const JobDesc& d) { return d.mword_begin; });
@@ -736,8 +724,6 @@ __global__ void __launch_bounds__(256) solid_morton_small(const __grid_constant_
 // Morton jobs with g < 32: clear the resolved flip table, one thread per resolve unit (the larger
 // grids' bricks clear their own words).
 __global__ void __launch_bounds__(256) solid_zero(const __grid_constant__ LaunchDesc L) {
-	pdl_wait();  // reads what the previous kernel of the sequence wrote
-	pdl_trigger();
 	const uint32_t unit_id = blockIdx.x * blockDim.x + threadIdx.x;
 	if (unit_id >= L.n_units) return;
 	const uint32_t j = job_search(L, unit_id, [](const JobDesc& d) { return (uint64_t)d.unit_begin; });
@@ -780,12 +766,12 @@ static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int col
 		solid_classify<P><<<L.n_tiles, kTile, 0, s>>>(L, tune.small_cols);
 		if ((e = cudaGetLastError()) != cudaSuccess) return e;
 		if (prof) (*prof)("solid_classify", s);
-		if ((e = launch_after(solid_cols<P>, (unsigned)cols_grid, kRowsThreads, 0, s, L)) != cudaSuccess) return e;
+		if ((e = launch_k(solid_cols<P>, (unsigned)cols_grid, kRowsThreads, 0, s, L)) != cudaSuccess) return e;
 		if (prof) (*prof)("solid_cols", s);
 	}
 	if (phases & kSolidResolve) {
 		if (L.n_units) {
-			if ((e = launch_after(solid_resolve, (L.n_units + 255) / 256, 256, 0, s, L)) != cudaSuccess) return e;
+			if ((e = launch_k(solid_resolve, (L.n_units + 255) / 256, 256, 0, s, L)) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_resolve", s);
 		}
 		if (L.n_mslabs) {
@@ -798,17 +784,17 @@ static cudaError_t launch_solid_t(const LaunchDesc& L, const Tune& tune, int col
 					return e;
 				attr_set[dev] = 1;
 			}
-			if ((e = launch_after(solid_morton_slab, (unsigned)L.n_mslabs, 256, L.slab_smem, s, L)) != cudaSuccess) return e;
+			if ((e = launch_k(solid_morton_slab, (unsigned)L.n_mslabs, 256, L.slab_smem, s, L)) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_morton_slab", s);
 		}
 		if (L.n_mbricks) {
-			if ((e = launch_after(solid_morton_brick, (unsigned)L.n_mbricks, 256, 0, s, L)) != cudaSuccess) return e;
+			if ((e = launch_k(solid_morton_brick, (unsigned)L.n_mbricks, 256, 0, s, L)) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_morton", s);
 		}
 		if (L.n_mwords) {
-			if ((e = launch_after(solid_morton_small, (unsigned)((L.n_mwords + 255) / 256), 256, 0, s, L)) != cudaSuccess)
+			if ((e = launch_k(solid_morton_small, (unsigned)((L.n_mwords + 255) / 256), 256, 0, s, L)) != cudaSuccess)
 				return e;
-			if ((e = launch_after(solid_zero, (L.n_units + 255) / 256, 256, 0, s, L)) != cudaSuccess) return e;
+			if ((e = launch_k(solid_zero, (L.n_units + 255) / 256, 256, 0, s, L)) != cudaSuccess) return e;
 			if (prof) (*prof)("solid_morton_small", s);
 		}
 	}
