@@ -902,19 +902,28 @@ def bench_batch(cv, torch, mix, default_tuning=None):
         jobs.append(cv.Job(info, torch.from_numpy(t.reshape(-1)).cuda(),
                            torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda"), s.morton, s.solid))
     n_tris = sum(int(j.info.n_triangles) for j in jobs)
-    reps = 5
+    reps = 10
+
+    stream = torch.cuda.current_stream()
+
+    def events_s(fn):
+        """Seconds per call of fn, between CUDA events on the launching stream."""
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / reps
 
     def time_plan():
         plan = cv.Plan(jobs, clear_tables=True)
         for _ in range(3):
             plan.launch()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            plan.launch()
-        torch.cuda.synchronize()
+        sec = events_s(plan.launch)
         plan.close()
-        return (time.perf_counter() - t0) / reps
+        return sec
 
     default_plan_ms = None
     if default_tuning:
@@ -931,10 +940,7 @@ def bench_batch(cv, torch, mix, default_tuning=None):
             (cv.voxelize_solid if j.solid else cv.voxelize)(j.info, j.triangles, j.table, j.morton)
             torch.cuda.synchronize()
     plain()
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        plain()
-    plain_s = (time.perf_counter() - t0) / reps
+    plain_s = events_s(plain)
     plan.close()
     return {"batch_256": {"meshes": 256, "triangles": n_tris, "plan_ms": plan_s * 1e3, "plain_ms": plain_s * 1e3,
                           "plan_meshes_s": 256 / plan_s, "plain_meshes_s": 256 / plain_s,
