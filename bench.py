@@ -549,7 +549,7 @@ def main():
     default_tuning = cv.get_tuning(local)
     tuned = autotune.autotune(local, reps=3)
     tuning = {"choice": {k: tuned[k] for k in autotune.KNOBS}, "default": default_tuning,
-              "tuning_set_ms": {"tuned": tuned["ms"], "default": tuned["default_ms"]},
+              "tuning_set_ms": {"tuned": tuned["ms"], "default": tuned["default_ms"]}, "min_gain": tuned["min_gain"],
               "seconds": tuned["seconds"]}
     tris = meshgen.icosphere(0, level=8)
     info = cv.make_voxinfo(tris, 512)

@@ -444,17 +444,22 @@ __global__ void __launch_bounds__(kRowsThreads) solid_cols(const __grid_constant
 		const uint64_t ncols = (uint64_t)(S.y1 - S.y0 + 1) * nzc;
 		const uint64_t c0 = (uint64_t)chunk * kColsPerItem;
 		const uint64_t c1 = umin64(ncols, c0 + kColsPerItem);
-		for (uint64_t c = c0 + lane; c < c1; c += 32) {
-			int y, z;
-			if (c1 <= 0xFFFFFFFFull) {
-				y = S.y0 + (int)((uint32_t)c / (uint32_t)nzc);
-				z = S.z0 + (int)((uint32_t)c % (uint32_t)nzc);
-			} else {
-				y = S.y0 + (int)(c / nzc);
-				z = S.z0 + (int)(c % nzc);
+		// column c is (y0 + c / nzc, z0 + c % nzc): one division for the lane's first column, then
+		// steps of 32 columns (dy rows and dz slices, carrying z into y)
+		const uint64_t cf = c0 + lane;
+		if (cf < c1) {  // (no lane enters when the range is empty: nzc may be 0 then)
+			int y = S.y0 + (int)(cf / nzc), z = S.z0 + (int)(cf % nzc);
+			const int dy = (int)(32u / nzc), dz = (int)(32u % nzc);
+			for (uint64_t c = cf; c < c1; c += 32) {
+				int xmax;
+				if (column_hit<P>(S, unit, y, z, morton, xmax)) record_hit(J.flips, grid, morton, y, z, xmax);
+				y += dy;
+				z += dz;
+				if (z > S.z1) {
+					z -= (int)nzc;
+					y++;
+				}
 			}
-			int xmax;
-			if (column_hit<P>(S, unit, y, z, morton, xmax)) record_hit(J.flips, grid, morton, y, z, xmax);
 		}
 	}
 }

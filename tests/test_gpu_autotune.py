@@ -35,11 +35,22 @@ def test_results_do_not_depend_on_the_thresholds(solid, morton):
         cv.set_tuning(0, **before)
 
 
+def test_autotune_keeps_thresholds_unless_clearly_faster(tmp_path):
+    """With a required gain no candidate can reach, the thresholds in effect stay."""
+    before = cv.get_tuning(0)
+    try:
+        r = at.autotune(0, cache_path=str(tmp_path / "t.json"), reps=1, min_gain=0.99)
+        assert {k: r[k] for k in at.KNOBS} == before == cv.get_tuning(0)
+        assert r["ms"] == r["default_ms"]
+    finally:
+        cv.set_tuning(0, **before)
+
+
 def test_autotune_applies_and_caches(tmp_path):
     before = cv.get_tuning(0)
     path = str(tmp_path / "tuning.json")
     try:
-        r = at.autotune(0, cache_path=path, reps=2)
+        r = at.autotune(0, cache_path=path, reps=2, min_gain=0.0)
         choice = {k: r[k] for k in at.KNOBS}
         assert cv.get_tuning(0) == choice
         assert r["ms"] <= min(c["ms"] for c in r["candidates"]) + 1e-9
