@@ -978,6 +978,29 @@ def copy_rates(torch, nbytes=1 << 30):
     return {"h2d_gbs": h2d / 1e9, "d2h_gbs": d2h / 1e9, "both_directions_gbs": duplex / 1e9}
 
 
+def link_jitter(torch, nbytes=4 << 20, n=1000):
+    """Distribution of single pinned copies of nbytes each way (one at a time, CUDA events): the
+    host-buffer serving arm moves a few MB per request, so a link that stalls now and then shows
+    up here as a long tail even with nothing else running in this process."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    out = {"bytes": nbytes, "copies": n}
+    for name, fn in (("h2d", lambda: d.copy_(h, non_blocking=True)), ("d2h", lambda: h.copy_(d, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for a, b in ev:
+            a.record(s)
+            fn()
+            b.record(s)
+        torch.cuda.synchronize()
+        ms = np.array([a.elapsed_time(b) for a, b in ev])
+        out[name] = {"p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+                     "max_ms": float(ms.max())}
+    return out
+
+
 def bench_serve(cv, meshgen, torch, mix, seconds, long_seconds, plan_meshes_s):
     """Open-loop serving of the 256-mesh distribution: Poisson arrivals, 40 GiB budget.  Two request
     kinds: host buffers (pinned triangles copied in, the table copied out) and device-resident
@@ -1035,13 +1058,15 @@ def bench_serve(cv, meshgen, torch, mix, seconds, long_seconds, plan_meshes_s):
         return res
 
     rates = copy_rates(torch)
+    jitter = link_jitter(torch)
     n = len(mix)
     per_req_in, per_req_out = in_bytes / n, out_bytes / n
     copy_cap = 1.0 / max(per_req_in / (rates["h2d_gbs"] * 1e9), per_req_out / (rates["d2h_gbs"] * 1e9),
                          (per_req_in + per_req_out) / (rates["both_directions_gbs"] * 1e9))
     out = {"budget_gib": 40, "seconds_per_rate": {"served 75% and 90% load": long_seconds, "other rates": seconds},
            "pool": "256-mesh mix (same as batch_256)",
-           "copy_rates": rates, "bytes_per_request": {"in": per_req_in, "out": per_req_out}}
+           "copy_rates": rates, "link_jitter_before": jitter,
+           "bytes_per_request": {"in": per_req_in, "out": per_req_out}}
     fr = (0.25, 0.5, 0.75, 0.9)
     long_fr = (0.75, 0.9)
     # capacity bursts of about half a second: a shorter burst overstated the host-buffer arm's
@@ -1050,6 +1075,7 @@ def bench_serve(cv, meshgen, torch, mix, seconds, long_seconds, plan_meshes_s):
     # the link's rates again after the host-buffer arms: the machine's host memory is shared, and a
     # drop here shows up as longer batch service times and queueing in the sweep above
     out["copy_rates_after_host_arms"] = copy_rates(torch)
+    out["link_jitter_after_host_arms"] = link_jitter(torch)
     host["roofline_meshes_s"] = min(copy_cap, plan_meshes_s)
     host["served_frac_of_roofline"] = host["served"]["capacity_meshes_s"] / host["roofline_meshes_s"]
     host["served_vs_plain_capacity"] = host["served"]["capacity_meshes_s"] / host["plain"]["capacity_meshes_s"]
