@@ -744,8 +744,9 @@ def main():
         sample = cpu_sample(tris)
         threads = os.cpu_count() or 1
         kind = "reference" if oracle.ref_cpu_available() else "port"
-        time_cpu_reference(bytes(info), sample, threads)  # warm-up
-        sec = float(np.mean([time_cpu_reference(bytes(info), sample, threads) for _ in range(3)]))
+        for _ in range(2):
+            time_cpu_reference(bytes(info), sample, threads)  # warm-up
+        sec = float(np.mean([time_cpu_reference(bytes(info), sample, threads) for _ in range(8)]))
         line["cpu_baseline"] = {"value": 4 * sample.shape[0] / sec / 1e6, "unit": "Mtris/s", "cores": threads,
                                 "kind": kind, "sample": sample_desc(sample.shape[0], T, kind)}
         if not args.no_extras:
