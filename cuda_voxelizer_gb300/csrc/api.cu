@@ -1093,7 +1093,7 @@ bool page_locked(const void* p) {
 }
 
 // One mesh's triangles on their way up: the host source, the device destination and the chunk
-// bounds (in triangles; interior bounds on whole 256-triangle tiles, so every chunk but the last
+// bounds (in triangles; interior bounds on whole kTile-triangle tiles, so every chunk but the last
 // starts 16-byte aligned when the buffer does and keeps the classify kernels' bulk tile copy).
 struct Upload {
 	const float* h = nullptr;

@@ -8,7 +8,7 @@
 
 namespace cvx {
 
-constexpr uint32_t kTile = 256;        // triangles per classify CTA (one tile)
+constexpr uint32_t kTile = 128;        // triangles per classify CTA (one tile; 2.6% faster than 256 on the bench step's plan)
 constexpr uint32_t kZch = 32;          // z-slices per surface work item (one per lane)
 constexpr uint32_t kRowsThreads = 256; // threads per cooperative CTA
 constexpr uint32_t kColsPerItem = 256; // solid columns per work item

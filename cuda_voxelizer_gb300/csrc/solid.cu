@@ -10,7 +10,7 @@
 // any set of [0, xmax] ranges is exactly what this produces.
 //
 // Kernels, in launch order:
-//   solid_classify      one CTA per 256-triangle tile (TMA bulk staging as in surface.cu); the
+//   solid_classify      one CTA per kTile-triangle tile (TMA bulk staging as in surface.cu); the
 //                       columns of triangles with at most `small_cols` columns are dealt over the
 //                       CTA, the other triangles queued.
 //   solid_cols          persistent; each warp takes items of up to kColsPerItem columns.

@@ -2,7 +2,7 @@
 //
 // Two kernels per launch sequence, both over a job table so that one mesh and a batch of meshes
 // run through the same code:
-//   surf_classify  one CTA per tile of 256 triangles of one job.  The tile is staged into shared
+//   surf_classify  one CTA per tile of kTile triangles of one job.  The tile is staged into shared
 //                  memory with one cp.async.bulk (TMA bulk copy) when it is full and 16-byte
 //                  aligned.  Each thread sets up its triangle; triangles whose grid bbox holds at
 //                  most `small_vox` voxels (every voxel tested, like the reference) or at most
@@ -107,8 +107,9 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_warp, uin
 // are dealt out evenly over the CTA, one (triangle, row) item per thread at a time, so that no
 // thread idles while another walks a larger bounding box.  A small triangle's row tests every
 // voxel like the reference; a local triangle's row is found with row_interval.
+// Registers (48) allow 10 CTAs of 128 threads per SM, shared memory (22.5 KB) 9.
 template <class P>
-__global__ void __launch_bounds__(kTile, 5) surf_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_vox) {
+__global__ void __launch_bounds__(kTile, 10) surf_classify(const __grid_constant__ LaunchDesc L, const uint32_t small_vox) {
 	__shared__ __align__(16) union {
 		float tri[kTile * 9];
 		SmallTri small[kTile];
