@@ -907,16 +907,20 @@ def bench_batch(cv, torch, mix, default_tuning=None):
 
     stream = torch.cuda.current_stream()
 
-    def events_s(fn):
-        """Seconds per call of fn, between CUDA events on the launching stream."""
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record(stream)
-        for _ in range(reps):
-            fn()
-        b.record(stream)
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / 1e3 / reps
+    def events_s(fn, blocks=5):
+        """Seconds per call of fn: the median over `blocks` blocks of `reps` calls, each block timed
+        between CUDA events on the launching stream."""
+        out = []
+        for _ in range(blocks):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b) / 1e3 / reps)
+        return float(np.median(out))
 
     def time_plan():
         plan = cv.Plan(jobs, clear_tables=True)
@@ -926,13 +930,16 @@ def bench_batch(cv, torch, mix, default_tuning=None):
         plan.close()
         return sec
 
+    plan_s = time_plan()
     default_plan_ms = None
     if default_tuning:
         tuned = cv.get_tuning(torch.cuda.current_device())
-        cv.set_tuning(torch.cuda.current_device(), **default_tuning)
-        default_plan_ms = time_plan() * 1e3
-        cv.set_tuning(torch.cuda.current_device(), **tuned)
-    plan_s = time_plan()
+        if tuned == default_tuning:
+            default_plan_ms = plan_s * 1e3  # the same thresholds: the same measurement
+        else:
+            cv.set_tuning(torch.cuda.current_device(), **default_tuning)
+            default_plan_ms = time_plan() * 1e3
+            cv.set_tuning(torch.cuda.current_device(), **tuned)
     plan = cv.Plan(jobs, clear_tables=True)
     # plain: what a caller of the reference drop-in does, one synchronous call per mesh
     def plain():
@@ -941,7 +948,7 @@ def bench_batch(cv, torch, mix, default_tuning=None):
             (cv.voxelize_solid if j.solid else cv.voxelize)(j.info, j.triangles, j.table, j.morton)
             torch.cuda.synchronize()
     plain()
-    plain_s = events_s(plain)
+    plain_s = events_s(plain, blocks=3)
     plan.close()
     return {"batch_256": {"meshes": 256, "triangles": n_tris, "plan_ms": plan_s * 1e3, "plain_ms": plain_s * 1e3,
                           "plan_meshes_s": 256 / plan_s, "plain_meshes_s": 256 / plain_s,
