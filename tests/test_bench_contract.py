@@ -1,0 +1,42 @@
+"""bench.py's output contract: stdout is exactly one JSON line with the keys the benchmark record
+needs.  The reference arm runs on the CPU (the reference's own CPU voxelizer where it was built on
+this machine, else the oracle port) and is checked here without a GPU; the engine arm needs one."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BASE_KEYS = {"metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+             "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"}
+
+
+def _run(args, timeout):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + args, capture_output=True, text=True,
+                       timeout=timeout, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, f"stdout must be one JSON line, got {len(lines)}: {r.stdout[:500]}"
+    return json.loads(lines[0])
+
+
+def test_reference_arm_prints_one_json_line():
+    line = _run(["--impl", "reference", "--steps", "1", "--warmup", "0", "--no-extras"], timeout=600)
+    assert line["impl"] == "reference"
+    assert BASE_KEYS <= set(line)
+    assert line["value"] > 0 and line["unit"] == "Mtris/s"
+    assert line["cpu_baseline"]["kind"] in ("reference", "port")
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+@pytest.mark.gpu
+def test_engine_arm_prints_one_json_line():
+    line = _run(["--steps", "3", "--warmup", "3", "--no-extras"], timeout=1200)
+    assert BASE_KEYS | {"roofline", "clocks", "gpu_launches", "tuning"} <= set(line)
+    assert line["value"] > 0 and line["gpu_launches"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] > 0 and line["e2e"]["d2h_bytes_per_step"] > 0
+    r = line["roofline"]
+    assert {"bound", "achieved", "peak", "unit", "frac", "traffic"} <= set(r)
+    assert line["clocks"]["sm_mhz"] is not None
