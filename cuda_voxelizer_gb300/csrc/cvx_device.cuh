@@ -274,23 +274,13 @@ __device__ __forceinline__ uint32_t compact3(uint64_t v) {
 	return (uint32_t)v;
 }
 
-// bfi.b32: dst with bits [pos, pos + len) replaced by the low len bits of src.
-__device__ __forceinline__ uint32_t bit_insert(uint32_t src, uint32_t dst, uint32_t pos, uint32_t len) {
-	uint32_t r;
-	asm("bfi.b32 %0, %1, %2, %3, %4;" : "=r"(r) : "r"(src), "r"(dst), "r"(pos), "r"(len));
-	return r;
-}
-
-// Place the x-nibble nib = (rw >> sh) & 0xF of a linear row word (x = 4X'..4X'+3 in MSB-first
-// order: nibble bit 3 is dx = 0) into Morton word `out`.  In a Morton word the code offset of
-// (dx, dy, dz) is (dx&1) | (dy&1)<<1 | dz<<2 | (dx>>1)<<3 | (dy>>1)<<4 and bits are MSB first, so
-// dx = 0, 1 land on bits 31, 30 and dx = 2, 3 on bits 23, 22, all shifted right by
-// shift = 2*(dy&1) + 4*dz + 16*(dy>>1).  The target bits must still be zero (every bit of a Morton
-// word comes from exactly one row nibble): two bit-field inserts replace masking, shifting and
-// OR-ing each half.
-__device__ __forceinline__ uint32_t place_nibble(uint32_t out, uint32_t rw, uint32_t sh, uint32_t shift) {
-	out = bit_insert(rw >> (sh + 2u), out, 30u - shift, 2u);  // nibble bits 3, 2 -> bits 31, 30 (>> shift)
-	return bit_insert(rw >> sh, out, 22u - shift, 2u);        // nibble bits 1, 0 -> bits 23, 22 (>> shift)
+// Morton bit mask of a 4-bit row nibble (x = 4X'..4X'+3 in MSB-first order: nibble bit 3 is dx = 0)
+// for dy = dz = 0.  In a Morton word the code offset of (dx, dy, dz) is
+// (dx&1) | (dy&1)<<1 | dz<<2 | (dx>>1)<<3 | (dy>>1)<<4, and bits are MSB first, so other (dy, dz)
+// shift the mask right by 2*(dy&1) + 4*dz + 16*(dy>>1).
+__device__ __forceinline__ uint32_t nibble_mask(uint32_t nib) {
+	// dx = 0, 1 (nibble bits 3, 2) -> offsets 0, 1 (bits 31, 30); dx = 2, 3 (bits 1, 0) -> offsets 8, 9
+	return ((nib & 0xCu) << 28) | ((nib & 0x3u) << 22);
 }
 
 

@@ -634,7 +634,8 @@ __global__ void __launch_bounds__(256) solid_morton_brick(const __grid_constant_
 #pragma unroll
 				for (uint32_t dy = 0; dy < 4; dy++) {
 					const uint32_t row = s_rows[((2 * Z + dz) * 32 + 4 * Y + dy) * 4 + xk];
-					out = place_nibble(out, row, 28u - 4u * X, 2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
+					const uint32_t nib = (row >> (28u - 4u * X)) & 0xFu;
+					out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 				}
 			xor_out(dest, m, out, (J.flags & JOB_TABLE_OVERWRITE) != 0);
 		}
@@ -697,7 +698,8 @@ __global__ void __launch_bounds__(256) solid_morton_slab(const __grid_constant__
 #pragma unroll
 			for (uint32_t dy = 0; dy < 4; dy++) {
 				const uint32_t rw = s_slab[slab_row((2 * Z + dz) * 16 + 4 * Y + dy, stride) + wsel];
-				out = place_nibble(out, rw, 28u - xoff, 2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
+				const uint32_t nib = (rw >> (28u - xoff)) & 0xFu;
+				out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 			}
 		xor_out(J.table, (blk << 7) + m, out, (J.flags & JOB_TABLE_OVERWRITE) != 0);
 	}

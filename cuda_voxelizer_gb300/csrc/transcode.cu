@@ -26,8 +26,8 @@ __global__ void __launch_bounds__(256) linear_to_morton(const uint32_t* __restri
 #pragma unroll
 		for (uint32_t dy = 0; dy < 4; dy++) {
 			const uint64_t bit = x0 + ((y0 + dy) << lg) + ((z0 + dz) << (2 * lg));
-			out = place_nibble(out, lin[bit >> 5], 28u - (uint32_t)(bit & 31u),
-			                   2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
+			const uint32_t nib = (lin[bit >> 5] >> (28u - (uint32_t)(bit & 31u))) & 0xFu;
+			out |= nibble_mask(nib) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 		}
 	mor[m] = out;
 }
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256) linear_to_morton_slab(const uint32_t* __r
 #pragma unroll
 			for (uint32_t dy = 0; dy < 4; dy++) {
 				const uint32_t rw = s_rows[slab_row((2 * Z + dz) * 16 + 4 * Y + dy, stride) + wsel];
-				out = place_nibble(out, rw, 28u - xoff, 2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
+				out |= nibble_mask((rw >> (28u - xoff)) & 0xFu) >> (2u * (dy & 1u) + 4u * dz + 16u * (dy >> 1));
 			}
 		mor[(slab_block(bx, by, bz) << 7) + m] = out;
 	}
