@@ -304,8 +304,7 @@ __device__ __forceinline__ bool row_interval_in(const SurfTri& S, const RowDirs&
 }
 
 // The x-dependent tests selected by `mask` at voxel x (bit i set = test i fails; bit layout of
-// fail_bits).  For callers whose mask is the same in every lane of a warp (one triangle per warp),
-// the tests outside the mask cost a uniform branch each instead of their evaluation.
+// fail_bits): the tests outside the mask are not evaluated.
 template <class P>
 __device__ __forceinline__ uint32_t fail_bits_masked(const SurfTri& S, const RowK& K, float ux, int x, uint32_t mask) {
 	const float px = __fmul_rn(__int2float_rn(x), ux);
@@ -339,48 +338,6 @@ __device__ __forceinline__ uint32_t fail_bits_masked(const SurfTri& S, const Row
 		}
 	}
 	return f & mask;
-}
-
-// row_interval_in for callers whose RowDirs are warp-uniform (one triangle per warp): each end
-// evaluates only the tests that bound it (lower-bound tests at the lower end, upper-bound tests at
-// the upper end).  Same result: an end is fixed by its own tests alone.
-template <class P>
-__device__ __forceinline__ bool row_interval_split(const SurfTri& S, const RowDirs& D, const RowK& K, float ux, int bx0,
-                                                   int bx1, int& xl, int& xh) {
-	const uint32_t dep = D.lo | D.hi;
-	const uint32_t cmask = ~dep & 0xFFu;
-	if (cmask && fail_bits_masked<P>(S, K, ux, bx0, cmask)) return false;
-	float elo = (float)bx0, ehi = (float)bx1;
-#pragma unroll
-	for (int i = 0; i < 8; i++) {
-		const uint32_t bit = 1u << i;
-		if (dep & bit) {
-			const float c = crossing(S, D, K.py, K.pz, i);
-			if (D.lo & bit) elo = fmaxf(elo, ceilf(c));
-			else ehi = fminf(ehi, floorf(c));
-		}
-	}
-	int e = (int)fminf(fmaxf(elo, (float)bx0), (float)bx1);
-	if (D.lo) {
-		if (!fail_bits_masked<P>(S, K, ux, e, D.lo)) {
-			while (e > bx0 && !fail_bits_masked<P>(S, K, ux, e - 1, D.lo)) e--;
-		} else {
-			do { e++; } while (e <= bx1 && fail_bits_masked<P>(S, K, ux, e, D.lo));
-			if (e > bx1) return false;
-		}
-	}
-	xl = e;
-	int f = (int)fminf(fmaxf(ehi, (float)xl), (float)bx1);
-	if (D.hi) {
-		if (!fail_bits_masked<P>(S, K, ux, f, D.hi)) {
-			while (f < bx1 && !fail_bits_masked<P>(S, K, ux, f + 1, D.hi)) f++;
-		} else {
-			do { f--; } while (f >= xl && fail_bits_masked<P>(S, K, ux, f, D.hi));
-			if (f < xl) return false;
-		}
-	}
-	xh = f;
-	return true;
 }
 
 // Exact pass interval of row (y, z) within the triangle's bbox [S.bx0, S.bx1].
