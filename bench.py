@@ -609,6 +609,7 @@ def main():
     total_ms = max_over_ranks(float(sum(times)), world)
     ms = total_ms / args.steps
     value = world * 4 * T * args.steps / (total_ms / 1e3) / 1e6
+    launches_per_step = plan.kernel_nodes()
     plan.close()
 
     # the same 4 calls through the per-call API: on 4 streams, and one after another on one stream
@@ -636,9 +637,7 @@ def main():
     cv.profile_enable(False)
     kernel_ms = {k: float(np.sum(v)) / reps for k, v in prof.items()}
     launches = {k: len(v) // reps for k, v in prof.items()}
-    # the engine's kernels in one step, counted by its events on the per-call form, plus the plan's
-    # one table-clearing kernel (the per-call form zeroes its tables with torch instead)
-    launches_per_step = sum(launches.values()) + 1
+    # the engine's kernels in one timed step: the plan graph's kernel nodes
     dom = max(kernel_ms, key=kernel_ms.get)
     # algorithmic bytes per launch: triangles read once (36 B each) + the table (g^3/8) for the
     # classify kernels; flip table read + table write (2 g^3/8) for the solid resolve.

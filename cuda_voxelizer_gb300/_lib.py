@@ -82,6 +82,7 @@ SIGNATURES = {
     "cvx_plan_create": (c_status, [ctypes.POINTER(CvxJob), u32, u32, ctypes.POINTER(vp)]),
     "cvx_plan_create_host": (c_status, [ctypes.POINTER(CvxHostJob), u32, u32, ctypes.POINTER(vp)]),
     "cvx_plan_launch": (c_status, [vp, vp]),
+    "cvx_plan_kernel_nodes": (c_status, [vp, ctypes.POINTER(u32)]),
     "cvx_plan_destroy": (c_status, [vp]),
     "cvx_server_create": (c_status, [ctypes.POINTER(CvxServerConfig), ctypes.POINTER(vp)]),
     "cvx_server_submit": (c_status, [vp, ctypes.POINTER(CvxServerRequest), ctypes.POINTER(u64)]),

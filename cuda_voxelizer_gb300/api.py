@@ -195,6 +195,12 @@ class Plan:
     def launch(self, stream=None) -> None:
         check(lib.cvx_plan_launch(self._h, _stream(stream)), "cvx_plan_launch")
 
+    def kernel_nodes(self) -> int:
+        """Kernel launches one launch() makes (the graph's kernel nodes)."""
+        n = ctypes.c_uint32()
+        check(lib.cvx_plan_kernel_nodes(self._h, ctypes.byref(n)), "cvx_plan_kernel_nodes")
+        return int(n.value)
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib.cvx_plan_destroy(self._h)
@@ -248,6 +254,12 @@ class HostPlan:
 
     def launch(self, stream=None) -> None:
         check(lib.cvx_plan_launch(self._h, _stream(stream)), "cvx_plan_launch")
+
+    def kernel_nodes(self) -> int:
+        """Kernel launches one launch() makes (the graph's kernel nodes)."""
+        n = ctypes.c_uint32()
+        check(lib.cvx_plan_kernel_nodes(self._h, ctypes.byref(n)), "cvx_plan_kernel_nodes")
+        return int(n.value)
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -1410,6 +1410,22 @@ cvx_status cvx_plan_launch(cvx_plan* p, cvx_stream_t stream) {
 	return CVX_OK;
 }
 
+cvx_status cvx_plan_kernel_nodes(const cvx_plan* p, uint32_t* n_kernels) {
+	if (!p || !p->graph || !n_kernels) return fail(CVX_ERR_INVALID_VALUE, "plan or output is null");
+	size_t n = 0;
+	CVX_CUDA(cudaGraphGetNodes(p->graph, nullptr, &n));
+	std::vector<cudaGraphNode_t> nodes(n);
+	if (n) CVX_CUDA(cudaGraphGetNodes(p->graph, nodes.data(), &n));
+	uint32_t k = 0;
+	for (size_t i = 0; i < n; i++) {
+		cudaGraphNodeType t;
+		CVX_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+		if (t == cudaGraphNodeTypeKernel) k++;
+	}
+	*n_kernels = k;
+	return CVX_OK;
+}
+
 cvx_status cvx_plan_destroy(cvx_plan* p) {
 	if (!p) return CVX_OK;
 	if (p->exec) cudaGraphExecDestroy(p->exec);

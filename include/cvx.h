@@ -145,6 +145,9 @@ typedef struct cvx_plan cvx_plan;
 #define CVX_PLAN_CLEAR_TABLES 1u
 cvx_status cvx_plan_create(const cvx_job* jobs, uint32_t n_jobs, uint32_t flags, cvx_plan** out);
 cvx_status cvx_plan_launch(cvx_plan* plan, cvx_stream_t stream);
+/* Number of kernel launches one cvx_plan_launch makes (the graph's kernel nodes; copies and memsets
+ * not counted).  Works for host-buffer plans too. */
+cvx_status cvx_plan_kernel_nodes(const cvx_plan* plan, uint32_t* n_kernels);
 cvx_status cvx_plan_destroy(cvx_plan* plan);
 
 /* Host-buffer plans: the reference's round trip (src/main.cpp:209-222 hands voxelize host-visible

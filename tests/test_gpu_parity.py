@@ -424,6 +424,26 @@ def test_plan_equals_single_calls_and_replays():
     plan.close()
 
 
+def test_plan_kernel_nodes():
+    """cvx_plan_kernel_nodes counts the graph's kernel launches: a clearing plan of one surface job
+    is its lane's clear, classify and rows kernels; one linear solid job (its table overwritten, not
+    cleared) is classify, columns and resolve; both together run as two lanes of three each."""
+    t = meshgen.torus(40)
+    info = info_of(t, 64)
+    td = torch.from_numpy(t.reshape(-1)).cuda()
+    a = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+    b = torch.zeros(cv.table_words(info), dtype=torch.int32, device="cuda")
+    for jobs, want in (([cv.Job(info, td, a, False, False)], 3), ([cv.Job(info, td, b, False, True)], 3),
+                       ([cv.Job(info, td, a, False, False), cv.Job(info, td, b, False, True)], 6)):
+        plan = cv.Plan(jobs, clear_tables=True)
+        assert plan.kernel_nodes() == want
+        plan.launch()
+        torch.cuda.synchronize()
+        plan.close()
+    assert torch.equal(a, run_engine(info, td, False, False)[:cv.table_words(info)])
+    assert torch.equal(b, run_engine(info, td, False, True)[:cv.table_words(info)])
+
+
 def test_plan_jobs_sharing_a_table_accumulate():
     """Jobs whose tables share words accumulate into them as repeated reference calls would: a
     clearing plan zeroes the shared table once, the surface job ORs, the solid job XORs (the plan
