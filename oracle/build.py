@@ -8,7 +8,8 @@
   tree is present (the development machine) the script stages the reference CPU voxelizer's source
   files into ``oracle/_ref/src`` and builds everything from the tree; elsewhere (the GPU machine, which
   receives ``oracle/_ref`` with the repository snapshot) it builds ``libref_cpu.so`` from the staged
-  sources, and the prebuilt device-code files are used as they are.  The reference tree is found
+  sources (and the reference's command-line program, relinked against libcvx.so), and the prebuilt
+  device-code files are used as they are.  The reference tree is found
   through the ``CVX_REFERENCE_ROOT`` environment variable, else as a checkout named ``reference``
   next to this repository.
 * ``oracle/_build/libref_gpu_runner.so``: ``oracle/ref_gpu_runner.cu``, the driver-API loader
@@ -68,7 +69,8 @@ def build_reference() -> None:
         _run(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
         return
     staged = os.path.join(REF_OUT, "src", "cpu_voxelizer.cpp")
-    if os.path.isfile(staged) and _stale(os.path.join(REF_OUT, "libref_cpu.so"), staged):
+    if os.path.isfile(staged) and (_stale(os.path.join(REF_OUT, "libref_cpu.so"), staged) or
+                                   _stale(os.path.join(REF_OUT, "cuda_voxelizer_relinked"), staged)):
         _run(["bash", os.path.join(HERE, "build_ref.sh"), "--staged"])
 
 
