@@ -44,9 +44,11 @@ def _shared_upload_jobs(tris, g):
 
 @pytest.mark.parametrize("n_chunks", [0, 1, 2, 3, 4, 64])
 def test_four_modes_one_upload_match_plain_calls(n_chunks):
-    tris = meshgen.icosphere(2, level=6)  # 81,920 triangles: 320 tiles, ragged over 3 and 64 chunks
+    tris = meshgen.icosphere(2, level=6)  # 81,920 triangles: 640 tiles, ragged over 3 and 64 chunks
     info, jobs = _shared_upload_jobs(tris, 256)
     plan = cv.HostPlan(jobs, n_chunks=n_chunks)
+    # every chunk's surface launches (classify + rows per job) and the two solid jobs' passes
+    assert plan.kernel_nodes() >= 2 * n_chunks + 3
     for _ in range(2):  # replays: each launch clears and recomputes every table
         plan.launch()
         torch.cuda.synchronize()

@@ -85,6 +85,24 @@ def test_server_refuses_a_request_larger_than_the_budget():
         assert srv.stats()["completed"] == 0
 
 
+def test_server_replay_stops_at_a_refused_request():
+    """A replay whose third request cannot fit the budget returns its error after the two it had
+    submitted completed (their latencies are written, the call does not hang), and the server
+    serves the next call normally."""
+    ok_info, ok_t, ok_tab = _host(meshgen.MeshSpec("torus", 1, 16, 64, False, False))
+    big_info, big_t, big_tab = _host(meshgen.MeshSpec("torus", 1, 16, 512, False, False))
+    pool = [cv.Server.request(ok_info, ok_t, ok_tab, False, False),
+            cv.Server.request(big_info, big_t, big_tab, False, False)]
+    with cv.Server(memory_budget_bytes=8 << 20, max_batch=4, max_inflight=1) as srv:
+        with pytest.raises(cv.CvxError) as e:
+            srv.replay(pool, np.array([0, 0, 1, 0]), np.zeros(4))
+        assert e.value.status == 3
+        assert srv.stats()["completed"] == 2
+        lat = srv.replay(pool, np.array([0, 0]), np.zeros(2))
+        assert np.all(lat > 0) and srv.stats()["completed"] == 4
+    assert torch.equal(ok_tab, _alone(ok_info, ok_t, False, False))
+
+
 def test_server_empty_mesh_returns_a_cleared_table():
     tris = np.zeros((0, 9), dtype=np.float32)
     info = cv.make_info((0, 0, 0), (1, 1, 1), 64, 0)
