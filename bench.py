@@ -424,6 +424,12 @@ def pc_soup(cv, meshgen, torch):
     return run
 
 
+def pc_soup_bricks(cv, meshgen, torch):
+    """the full soup with the brick rasterizer on (brick_pairs = 16)"""
+    cv.set_tuning(torch.cuda.current_device(), brick_pairs=16)
+    return pc_soup(cv, meshgen, torch)
+
+
 def pc_soup200k(cv, meshgen, torch):
     """the first 200,000 triangles of that soup at 1024^3 (a small case of surf_rows and of the brick
     kernels), with the device's current tuning"""
@@ -509,7 +515,8 @@ def pc_io(cv, meshgen, torch):
     return run
 
 
-PROFILE_CASES = {"ico8": pc_ico8, "ico8_plan": pc_ico8_plan, "soup": pc_soup, "soup200k": pc_soup200k,
+PROFILE_CASES = {"ico8": pc_ico8, "ico8_plan": pc_ico8_plan, "soup": pc_soup, "soup_bricks": pc_soup_bricks,
+                 "soup200k": pc_soup200k,
                  "soup200k_bricks": pc_soup200k_bricks,
                  "batch": pc_batch, "batch_g512": pc_batch_g512, "batch_g512_solid": pc_batch_g512_solid,
                  "io": pc_io}
