@@ -47,6 +47,8 @@ import numpy as np  # noqa: E402
 MODES = [(False, False), (True, False), (False, True), (True, True)]  # (morton, solid)
 METRIC = "Mtris/s voxelized (icosphere 1.31M tris, 512^3, surface+solid x linear+Morton)"
 SAMPLE_FRACTION = 32
+THREADS_NOTE = ("the fastest thread count on this host (seconds per thread count on a 1/128 calibration "
+                "sample in threads_tried_s): the reference's OpenMP loop takes a critical section per bit")
 
 
 def parse(argv=None):
@@ -300,6 +302,18 @@ def sample_desc(n, total, kind):
                "the oracle port of src/cpu_voxelizer.cpp (OpenMP parallel-for, a critical section per bit)"))
 
 
+def _omp_threads(n):
+    """Thread count of the OpenMP parallel regions this thread starts next, in the OpenMP runtime
+    the reference's CPU build links (libgomp): OMP_NUM_THREADS is read only once, at its first
+    parallel region."""
+    import ctypes
+    os.environ["OMP_NUM_THREADS"] = str(n)
+    try:
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(ctypes.c_int(int(n)))
+    except (OSError, AttributeError):
+        pass
+
+
 def time_cpu_reference(info_bytes, sample, threads):
     """The reference CPU algorithm over the 4 modes on a sample of the mesh (same grid, the
     sample's triangle count); returns seconds.  Runs the reference's own build where it exists on
@@ -307,7 +321,7 @@ def time_cpu_reference(info_bytes, sample, threads):
     section per bit write)."""
     import oracle
     info_s = oracle.with_count(info_bytes, sample.shape[0])
-    os.environ["OMP_NUM_THREADS"] = str(threads)
+    _omp_threads(threads)
     t0 = time.perf_counter()
     for morton, solid in MODES:
         if oracle.ref_cpu_available():
@@ -315,6 +329,21 @@ def time_cpu_reference(info_bytes, sample, threads):
         else:
             oracle.voxelize_omp(info_s, sample, morton=morton, solid=solid, threads=threads)
     return time.perf_counter() - t0
+
+
+def cpu_threads(info_bytes, tris, max_threads):
+    """The thread count the CPU legs run the reference's algorithm with: the fastest of 1, 2, 4, ...
+    and all of this host's threads on a 1/128 sample (best of two runs each).  Its OpenMP loop takes
+    a critical section for every bit it sets, so on this workload more threads can be slower than
+    one; timing it with all threads regardless would understate the reference.  Returns (threads,
+    {threads: seconds on the calibration sample})."""
+    small = np.ascontiguousarray(tris[:max(1024, tris.shape[0] // 128)])
+    cands = sorted({t for t in (1, 2, 4, 8, 16, 32, 64) if t < max_threads} | {max_threads})
+    secs = {}
+    for t in cands:
+        time_cpu_reference(info_bytes, small, t)
+        secs[t] = min(time_cpu_reference(info_bytes, small, t) for _ in range(2))
+    return min(secs, key=secs.get), {str(t): round(v, 4) for t, v in secs.items()}
 
 
 def load_meshgen():
@@ -349,7 +378,7 @@ def run_reference_arm(args, rank, world):
     meshgen = load_meshgen()
     tris = meshgen.icosphere(0, level=8)
     info = reference_voxinfo(tris, 512)
-    threads = os.cpu_count() or 1
+    threads, tried = cpu_threads(info, tris, os.cpu_count() or 1)
     kind = "reference" if oracle.ref_cpu_available() else "port"
     sample = cpu_sample(tris)
     n = sample.shape[0]
@@ -365,7 +394,8 @@ def run_reference_arm(args, rank, world):
                                    "per step", "gridsize": 512, "triangles": int(tris.shape[0]),
                        "sample_triangles": n, "sample": f"first 1/{SAMPLE_FRACTION} of the triangles"},
             "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": threads, "kind": kind,
-                             "sample": sample_desc(n, tris.shape[0], kind)},
+                             "sample": sample_desc(n, tris.shape[0], kind), "threads_tried_s": tried,
+                             "threads_note": THREADS_NOTE},
             "e2e": {"value": value, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if not args.no_extras:
         try:
@@ -748,13 +778,14 @@ def main():
     if rank == 0:
         import oracle
         sample = cpu_sample(tris)
-        threads = os.cpu_count() or 1
+        threads, tried = cpu_threads(bytes(info), tris, os.cpu_count() or 1)
         kind = "reference" if oracle.ref_cpu_available() else "port"
         for _ in range(2):
             time_cpu_reference(bytes(info), sample, threads)  # warm-up
         sec = float(np.mean([time_cpu_reference(bytes(info), sample, threads) for _ in range(8)]))
         line["cpu_baseline"] = {"value": 4 * sample.shape[0] / sec / 1e6, "unit": "Mtris/s", "cores": threads,
-                                "kind": kind, "sample": sample_desc(sample.shape[0], T, kind)}
+                                "kind": kind, "sample": sample_desc(sample.shape[0], T, kind),
+                                "threads_tried_s": tried, "threads_note": THREADS_NOTE}
         if not args.no_extras:
             extras.update(bench_soup(cv, meshgen, torch, stream, flush))
             specs = meshgen.batch_mix(0, 256)
