@@ -288,15 +288,45 @@ def step_roofline(cv, torch, T, table_bytes, hbm_gbs, ms_per_step):
             "frac": t_roof / (ms_per_step / 1e3)}
 
 
-def cpu_sample(tris):
-    """The CPU legs' bounded sample: the first 1/32 of the mesh's triangles (the same sample for the
-    engine line's cpu_baseline and for --impl reference)."""
-    n = tris.shape[0] // SAMPLE_FRACTION
+def cpu_sample(tris, fraction=SAMPLE_FRACTION):
+    """The first 1/fraction of the mesh's triangles (fraction 1: the whole mesh)."""
+    n = tris.shape[0] // fraction
     return np.ascontiguousarray(tris[:n])
 
 
-def sample_desc(n, total, kind):
-    return (f"first {n} of {total} triangles (1/{SAMPLE_FRACTION}) of the same mesh and grid, 4 modes; "
+def cpu_work(info_bytes, tris):
+    """The triangles the CPU legs give the reference's code in each of the 4 modes: all of them for
+    surface; for solid, those oracle/ref_safety.py keeps (about 1% of the icosphere is dropped: the
+    reference's solid loop can start its run at a negative or out-of-table x on the others and
+    write outside its table -- its CPU loop stores a negative xmax in an unsigned int)."""
+    import oracle
+    from oracle.ref_safety import safe_triangles
+    out = []
+    for morton, solid in MODES:
+        if solid:
+            keep = safe_triangles(tris, oracle.with_count(info_bytes, tris.shape[0]), morton)
+            out.append(np.ascontiguousarray(tris[keep]))
+        else:
+            out.append(tris)
+    return out
+
+
+def cpu_fraction(pass_s, passes, budget_s):
+    """The largest power-of-two share 1/f of the workload (f = 1, 2, 4, ..., SAMPLE_FRACTION) whose
+    `passes` runs fit `budget_s`, given the estimated seconds of one pass over the whole workload."""
+    f = 1
+    while f < SAMPLE_FRACTION and passes * pass_s / f > budget_s:
+        f *= 2
+    return f
+
+
+def sample_desc(work, total, kind, fraction=SAMPLE_FRACTION):
+    what = ("the whole workload" if fraction == 1 else
+            f"the first 1/{fraction} of the triangles of the same mesh and grid")
+    solid = work[2].shape[0]
+    return (f"{what}, 4 modes: {work[0].shape[0]} triangles per surface mode, {solid} per solid mode (the "
+            f"{work[0].shape[0] - solid} the reference's solid loop could run outside its table left out, "
+            f"oracle/ref_safety.py); "
             + ("the reference's own src/cpu_voxelizer.cpp built on this host (OpenMP parallel-for, a critical "
                "section per bit)" if kind == "reference" else
                "the oracle port of src/cpu_voxelizer.cpp (OpenMP parallel-for, a critical section per bit)"))
@@ -314,20 +344,19 @@ def _omp_threads(n):
         pass
 
 
-def time_cpu_reference(info_bytes, sample, threads):
-    """The reference CPU algorithm over the 4 modes on a sample of the mesh (same grid, the
-    sample's triangle count); returns seconds.  Runs the reference's own build where it exists on
-    this host, else the oracle port of it (same structure: OpenMP over triangles, a critical
-    section per bit write)."""
+def time_cpu_reference(info_bytes, work, threads):
+    """The reference CPU algorithm over the 4 modes, mode i on the triangles work[i] (cpu_work; same
+    grid); returns seconds.  Runs the reference's own build where it exists on this host, else the
+    oracle port of it (same structure: OpenMP over triangles, a critical section per bit write)."""
     import oracle
-    info_s = oracle.with_count(info_bytes, sample.shape[0])
     _omp_threads(threads)
+    infos = [oracle.with_count(info_bytes, w.shape[0]) for w in work]
     t0 = time.perf_counter()
-    for morton, solid in MODES:
+    for (morton, solid), w, info_s in zip(MODES, work, infos):
         if oracle.ref_cpu_available():
-            oracle.ref_cpu_voxelize(info_s, sample, morton=morton, solid=solid, quiet=True)
+            oracle.ref_cpu_voxelize(info_s, w, morton=morton, solid=solid, quiet=True)
         else:
-            oracle.voxelize_omp(info_s, sample, morton=morton, solid=solid, threads=threads)
+            oracle.voxelize_omp(info_s, w, morton=morton, solid=solid, threads=threads)
     return time.perf_counter() - t0
 
 
@@ -336,14 +365,16 @@ def cpu_threads(info_bytes, tris, max_threads):
     and all of this host's threads on a 1/128 sample (best of two runs each).  Its OpenMP loop takes
     a critical section for every bit it sets, so on this workload more threads can be slower than
     one; timing it with all threads regardless would understate the reference.  Returns (threads,
-    {threads: seconds on the calibration sample})."""
-    small = np.ascontiguousarray(tris[:max(1024, tris.shape[0] // 128)])
+    {threads: seconds on the calibration sample}, estimated seconds of one pass over the whole
+    workload at that thread count)."""
+    small = cpu_work(info_bytes, np.ascontiguousarray(tris[:max(1024, tris.shape[0] // 128)]))
     cands = sorted({t for t in (1, 2, 4, 8, 16, 32, 64) if t < max_threads} | {max_threads})
     secs = {}
     for t in cands:
         time_cpu_reference(info_bytes, small, t)
         secs[t] = min(time_cpu_reference(info_bytes, small, t) for _ in range(2))
-    return min(secs, key=secs.get), {str(t): round(v, 4) for t, v in secs.items()}
+    best = min(secs, key=secs.get)
+    return best, {str(t): round(v, 4) for t, v in secs.items()}, secs[best] * tris.shape[0] / small[0].shape[0]
 
 
 def load_meshgen():
@@ -378,23 +409,27 @@ def run_reference_arm(args, rank, world):
     meshgen = load_meshgen()
     tris = meshgen.icosphere(0, level=8)
     info = reference_voxinfo(tris, 512)
-    threads, tried = cpu_threads(info, tris, os.cpu_count() or 1)
+    threads, tried, pass_s = cpu_threads(info, tris, os.cpu_count() or 1)
     kind = "reference" if oracle.ref_cpu_available() else "port"
-    sample = cpu_sample(tris)
-    n = sample.shape[0]
+    # each step the whole workload when the run's warm-up and timed steps fit about two minutes,
+    # else the largest power-of-two share of it that does
+    frac = cpu_fraction(pass_s, args.steps + args.warmup, 120.0)
+    work = cpu_work(info, cpu_sample(tris, frac))
+    n = sum(w.shape[0] for w in work)
     for _ in range(args.warmup):
-        time_cpu_reference(info, sample, threads)
-    ts = [time_cpu_reference(info, sample, threads) for _ in range(args.steps)]
+        time_cpu_reference(info, work, threads)
+    ts = [time_cpu_reference(info, work, threads) for _ in range(args.steps)]
     sec = float(np.mean(ts))
-    value = 4 * n / sec / 1e6
+    value = n / sec / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mtris/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced icosphere)",
             "config": {"workload": "icosphere level 8 (1,310,720 tris) at 512^3; surface+solid x linear+Morton "
                                    "per step", "gridsize": 512, "triangles": int(tris.shape[0]),
-                       "sample_triangles": n, "sample": f"first 1/{SAMPLE_FRACTION} of the triangles"},
+                       "triangles_per_step": n,
+                       "sample": "the whole workload" if frac == 1 else f"first 1/{frac} of the triangles"},
             "cpu_baseline": {"value": value, "unit": "Mtris/s", "cores": threads, "kind": kind,
-                             "sample": sample_desc(n, tris.shape[0], kind), "threads_tried_s": tried,
+                             "sample": sample_desc(work, tris.shape[0], kind, frac), "threads_tried_s": tried,
                              "threads_note": THREADS_NOTE},
             "e2e": {"value": value, "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if not args.no_extras:
@@ -777,14 +812,14 @@ def main():
 
     if rank == 0:
         import oracle
-        sample = cpu_sample(tris)
-        threads, tried = cpu_threads(bytes(info), tris, os.cpu_count() or 1)
+        threads, tried, pass_s = cpu_threads(bytes(info), tris, os.cpu_count() or 1)
         kind = "reference" if oracle.ref_cpu_available() else "port"
-        for _ in range(2):
-            time_cpu_reference(bytes(info), sample, threads)  # warm-up
-        sec = float(np.mean([time_cpu_reference(bytes(info), sample, threads) for _ in range(8)]))
-        line["cpu_baseline"] = {"value": 4 * sample.shape[0] / sec / 1e6, "unit": "Mtris/s", "cores": threads,
-                                "kind": kind, "sample": sample_desc(sample.shape[0], T, kind),
+        frac = cpu_fraction(pass_s, 3, 20.0)  # about 10-20 s of CPU work: the whole workload if it fits
+        work = cpu_work(bytes(info), cpu_sample(tris, frac))
+        time_cpu_reference(bytes(info), work, threads)  # warm-up
+        sec = float(np.mean([time_cpu_reference(bytes(info), work, threads) for _ in range(2)]))
+        line["cpu_baseline"] = {"value": sum(w.shape[0] for w in work) / sec / 1e6, "unit": "Mtris/s",
+                                "cores": threads, "kind": kind, "sample": sample_desc(work, T, kind, frac),
                                 "threads_tried_s": tried, "threads_note": THREADS_NOTE}
         if not args.no_extras:
             extras.update(bench_soup(cv, meshgen, torch, stream, flush))

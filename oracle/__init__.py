@@ -254,7 +254,12 @@ def ref_cpu_voxelize(info: bytes, tris, morton: bool = False, solid: bool = Fals
         raise RuntimeError("reference CPU build not available on this machine")
     t = _soup(tris, info)
     ib = ctypes.create_string_buffer(bytes(info), 64)
-    table = np.zeros(table_words(info), dtype=np.uint32)
+    # The reference's solid loop can run past its table for nearly x-parallel triangles near the
+    # table's end (its float32 xmax exceeds the grid; the reference writes outside its buffer
+    # there): a guard area as large as the table keeps those writes in memory this call owns.
+    words = table_words(info)
+    buf = np.zeros(2 * words + 1024, dtype=np.uint32)
+    table = buf[:words]
     fn = L.ref_cpu_voxelize_solid if solid else L.ref_cpu_voxelize
     if quiet:
         with _stdout_to_devnull():

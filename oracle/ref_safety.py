@@ -1,4 +1,5 @@
-"""Keep the reference's solid kernel inside its table (test infrastructure).
+"""Keep the reference's solid code inside its table (test infrastructure: the checker, never the
+product).
 
 The reference kernel voxelize_triangle_solid (src/voxelize_solid.cu:73-145) never clips x: it XORs
 bits x = 0..xmax of each hit column, with xmax = int(get_x_coordinate(...) / unit.x - 0.5)
@@ -22,6 +23,13 @@ produce such a write, using float64 geometry with generous margins:
     triangle's yz projection or within 1e-3 world units of an edge: the reference's 1e-6 tolerance
     on an edge's cross product), the plane's x (plus a 16-voxel margin) reaches g - 1 (Morton) or the run
     x + y*gx + z*gx*gy (plus margin) reaches the end of the table (linear).
+The reference's CPU solid loop (src/cpu_voxelizer.cpp:293-296) has the same xmax and one more
+hazard: it stores int(...) into an unsigned int, so a negative xmax becomes a loop of about 2^32
+iterations writing far outside the table (the displaced icosphere has such a triangle, n.x = -7.6e-5).
+The triangles kept here are far from both (the filter drops every |n.x| < 1e-2, and elsewhere the
+plane's x at a counted column is inside the mesh's bbox), so the benchmark's CPU legs run the
+reference's solid code on them.
+
 The engine itself clips these writes (x to the grid in Morton order, the run to the table in linear
 order), so it needs no such filter.
 """

@@ -28,7 +28,7 @@ import oracle  # noqa: E402
 from cuda_voxelizer_gb300 import _lib  # noqa: E402
 from cuda_voxelizer_gb300 import api as cv  # noqa: E402
 from cuda_voxelizer_gb300 import meshgen  # noqa: E402
-from ref_safety import safe_triangles  # noqa: E402
+from oracle.ref_safety import safe_triangles  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -113,7 +113,7 @@ def test_cxx_symbols_on_managed_memory(ref, capfd, name, morton, solid):
     info = cv.make_voxinfo(tris, g)
     if solid:
         # the reference solid kernel writes outside its table for some near-x-parallel triangles
-        # (tests/ref_safety.py); both sides get the mesh without them
+        # (oracle/ref_safety.py); both sides get the mesh without them
         tris = np.ascontiguousarray(tris[safe_triangles(tris, bytes(info), morton)])
         info = cv.VoxInfo.from_buffer_copy(bytes(info))
         info.n_triangles = tris.shape[0]

@@ -20,7 +20,7 @@ from cuda_voxelizer_gb300 import api as cv  # noqa: E402
 from cuda_voxelizer_gb300 import meshgen  # noqa: E402
 from golden_data import arrays, manifest, mesh, table_keys  # noqa: E402
 import tie_trace  # noqa: E402
-from ref_safety import safe_triangles  # noqa: E402
+from oracle.ref_safety import safe_triangles  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -56,7 +56,7 @@ _SAFE = {}
 
 def for_reference(tris, info, morton, solid):
     """The reference solid kernel writes outside its table for some near-x-parallel triangles
-    (tests/ref_safety.py); both implementations get the mesh without them."""
+    (oracle/ref_safety.py); both implementations get the mesh without them."""
     if not solid:
         return tris, info
     import hashlib

@@ -6,7 +6,7 @@
 * The 256-mesh uneven mix (meshgen.batch_mix(0, 256): tori and displaced icospheres of 1k-500k
   triangles, grids 64-512, surface:solid 3:1, linear:Morton 1:1) as one clearing plan, every table
   against the reference kernels.
-* Solid voxelization on the triangles tests/ref_safety.py removes before the reference solid kernel
+* Solid voxelization on the triangles oracle/ref_safety.py removes before the reference solid kernel
   may run (nearly x-parallel or nearly degenerate triangles, whose float32 xmax can leave the grid:
   the reference kernel then writes outside its table, and once faulted the GPU).  Those triangles
   are checked against the oracle in GPU-arithmetic mode instead -- the reference kernel's fused
@@ -28,7 +28,7 @@ torch = pytest.importorskip("torch")
 import oracle  # noqa: E402
 from cuda_voxelizer_gb300 import api as cv  # noqa: E402
 from cuda_voxelizer_gb300 import meshgen  # noqa: E402
-from ref_safety import safe_triangles  # noqa: E402
+from oracle.ref_safety import safe_triangles  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
