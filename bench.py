@@ -18,15 +18,18 @@ Keys beyond the base contract:
                (MEASURED_PEAKS.json), with DRAM traffic from the committed ncu summary when present.
   cpu_baseline the reference's own CPU voxelizer (src/cpu_voxelizer.cpp, OpenMP with a critical section
                per bit, built on this host by oracle/build_ref.sh; the oracle port where that build
-               is missing) on the first 1/32 of the same triangles, all 4 modes.
+               is missing) on the same workload, all 4 modes, at the host's fastest thread count
+               (the whole mesh when it fits about 20 s; the solid modes without the triangles its
+               solid loop could run outside its table, oracle/ref_safety.py).
   extras       the triangle-size stress soup (2M triangles at 1024^3; the reference CUDA kernel rebuilt
                for sm_103a is timed on it by --impl reference), the 256-mesh batched workload against
                plain per-mesh calls, and open-loop serving of that mix (Poisson arrivals, 40 GiB
                budget, p50/p99) against one-request-at-a-time launches.
 
 --impl reference times the reference's CPU implementation of the path (its own build, as for
-cpu_baseline) on the same 1/32 sample, one sample per step; it builds its voxinfo with the oracle's
-restatement of the reference's setup and loads nothing of the engine.
+cpu_baseline) on the same workload, the whole mesh per step whenever the run fits about two minutes
+(else the first 1/2^k of the triangles); it builds its voxinfo with the oracle's restatement of the
+reference's setup and loads nothing of the engine.
 """
 from __future__ import annotations
 
