@@ -40,3 +40,28 @@ def test_engine_arm_prints_one_json_line():
     r = line["roofline"]
     assert {"bound", "achieved", "peak", "unit", "frac", "traffic"} <= set(r)
     assert line["clocks"]["sm_mhz"] is not None
+
+
+def test_cpu_leg_sizing():
+    """The CPU legs run the whole workload when the run fits its budget, else the largest
+    power-of-two share that does (at most 1/32)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.cpu_fraction(4.0, 25, 120.0) == 1
+    assert bench.cpu_fraction(4.5, 410, 120.0) == 16
+    assert bench.cpu_fraction(1e9, 10, 1.0) == bench.SAMPLE_FRACTION
+
+
+def test_cpu_work_drops_only_unsafe_solid_triangles():
+    sys.path.insert(0, ROOT)
+    import bench
+    import oracle
+    meshgen = bench.load_meshgen()
+    tris = meshgen.icosphere(0, level=5)
+    info = bench.reference_voxinfo(tris, 128)
+    work = bench.cpu_work(info, tris)
+    assert work[0].shape == tris.shape and work[1].shape == tris.shape  # surface modes: every triangle
+    for w, (morton, solid) in zip(work, bench.MODES):
+        if solid:
+            from oracle.ref_safety import safe_triangles
+            assert w.shape[0] == int(safe_triangles(tris, oracle.with_count(info, tris.shape[0]), morton).sum())
