@@ -65,3 +65,14 @@ def test_cpu_work_drops_only_unsafe_solid_triangles():
         if solid:
             from oracle.ref_safety import safe_triangles
             assert w.shape[0] == int(safe_triangles(tris, oracle.with_count(info, tris.shape[0]), morton).sum())
+
+
+def test_smoke_resolves_its_imports_without_a_gpu():
+    """smoke() imports the package, the oracle and the triangle filter before it asks for cuda:0;
+    on a machine without a GPU it must get that far and stop at its own check."""
+    code = ("import torch, __graft_entry__ as g\n"
+            "assert not torch.cuda.is_available()\n"
+            "try:\n    g.smoke()\nexcept AssertionError as e:\n    print('stopped:', e)\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "stopped: smoke() needs cuda:0" in r.stdout
