@@ -11,7 +11,10 @@ Keys beyond the base contract:
   e2e          the same metric through the public host-buffer path: pinned host triangles copied in,
                four voxelizations, four tables copied out, all inside the timed region, as one
                cvx_plan_create_host graph launch per step (chunked upload, tables read back as soon
-               as each is complete); plain_calls is the same round trip through per-call API calls.
+               as each is complete), K steps back to back on two such plans with their own buffers,
+               launched on two streams in turn (one step's upload overlaps the previous step's
+               read-back); single_step is one plan's round trip timed alone, plain_calls the same
+               round trip through per-call API calls.
   step_per_call the four drop-in calls on four streams, enqueued from Python every step.
   step_sequential the four drop-in calls one after another on one stream.
   roofline     the step's dominant kernel against the measured HBM copy bandwidth
@@ -50,6 +53,7 @@ import numpy as np  # noqa: E402
 MODES = [(False, False), (True, False), (False, True), (True, True)]  # (morton, solid)
 METRIC = "Mtris/s voxelized (icosphere 1.31M tris, 512^3, surface+solid x linear+Morton)"
 SAMPLE_FRACTION = 32
+E2E_SLOTS = 2  # host plans in flight in the e2e measurement
 THREADS_NOTE = ("the fastest thread count on this host (seconds per thread count on a 1/128 calibration "
                 "sample in threads_tried_s): the reference's OpenMP loop takes a critical section per bit")
 
@@ -734,16 +738,40 @@ def main():
     h_tris = torch.from_numpy(tris.reshape(-1)).pin_memory()
     h_out = [torch.empty(W, dtype=torch.int32).pin_memory() for _ in MODES]
 
-    # One host-buffer plan (cvx_plan_create_host) is the step: the triangles go up in 2 chunks, the
-    # surface jobs voxelize each chunk as it lands, the solid jobs follow, and each table is copied
-    # down as soon as it is complete.  The link (about 200 GB/s each way here) bounds the step, so
-    # the plan's job is to hide the kernels under the copies; its graph launch also takes the
-    # host's per-call enqueue time out of the step.
-    host_plan = cv.HostPlan([cv.HostJob(info, h_tris, d_tris, out, tab, morton, solid)
-                             for (morton, solid), tab, out in zip(MODES, tables, h_out)], n_chunks=2)
+    # A host-buffer plan (cvx_plan_create_host) is one step's round trip: the triangles go up in 2
+    # chunks, the surface jobs voxelize each chunk as it lands, the solid jobs follow, and each table
+    # is copied down as soon as it is complete; its graph launch also takes the host's per-call
+    # enqueue time out of the step.  Steps run back to back on E2E_SLOTS such plans, each with its
+    # own device buffers and host tables, launched on their own streams in turn: a step's upload and
+    # kernels run while the step before it is still copying its tables down, so the host link
+    # (about 200 GB/s each way here, 333 GB/s both ways at once) is busy in both directions.  A
+    # third slot measured no faster than two.
+    slots = []
+    for _ in range(E2E_SLOTS):
+        d_k = torch.empty_like(d_tris)
+        tabs_k = [torch.empty_like(t) for t in tables]
+        outs_k = [torch.empty(W, dtype=torch.int32).pin_memory() for _ in MODES]
+        plan_k = cv.HostPlan([cv.HostJob(info, h_tris, d_k, out, tab, morton, solid)
+                              for (morton, solid), tab, out in zip(MODES, tabs_k, outs_k)], n_chunks=2)
+        slots.append((plan_k, torch.cuda.Stream(), outs_k, d_k, tabs_k))
+
+    def e2e_steps(n):
+        """n steps back to back, step k on slot k % E2E_SLOTS; returns the events around them."""
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for slot in slots:
+            slot[1].wait_event(a)
+        for k in range(n):
+            plan_k, s = slots[k % E2E_SLOTS][:2]
+            plan_k.launch(s)
+        for slot in slots:
+            stream.wait_stream(slot[1])
+        b.record(stream)
+        return a, b
 
     def e2e_step():
-        host_plan.launch()
+        slots[0][0].launch()
 
     def e2e_plain_step():
         d_tris.copy_(h_tris, non_blocking=True)
@@ -768,11 +796,13 @@ def main():
         plain_times.append(a.elapsed_time(b))
     plain_e2e_ms = float(np.mean(plain_times))
 
+    # one host plan, one step at a time (L2 flushed and the device idle before each): the round trip's
+    # latency
     for _ in range(3):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_times = []
-    for _ in range(args.steps):
+    single_times = []
+    for _ in range(min(args.steps, 100)):
         flush.fill_(1)
         torch.cuda.synchronize()
         a = torch.cuda.Event(enable_timing=True)
@@ -781,26 +811,58 @@ def main():
         e2e_step()
         b.record(stream)
         torch.cuda.synchronize()
-        e2e_times.append(a.elapsed_time(b))
-    # the pipelined path must return exactly what the plain calls compute
+        single_times.append(a.elapsed_time(b))
+    single_ms = max_over_ranks(float(np.mean(single_times)), world)
+
+    # the timed e2e: K steps back to back over the slots
+    e2e_steps(max(3, args.warmup) * E2E_SLOTS)
+    flush.fill_(1)
+    torch.cuda.synchronize()
+    barrier(world)
+    a, b = e2e_steps(args.steps)
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_ms = max_over_ranks(a.elapsed_time(b) / args.steps, world)
+
+    # every host table must hold exactly what the device-resident step computes
     step()
     torch.cuda.synchronize()
-    for k, (tab, out) in enumerate(zip(tables, h_out)):
-        if not torch.equal(tab.cpu(), out):
-            raise RuntimeError(f"e2e table {k} differs from the device-resident result")
-    e2e_ms = max_over_ranks(float(np.mean(e2e_times)), world)
-    host_plan.close()
-    # the link's bound on the step: every byte up, then every byte down (no table can leave before
-    # the last triangle has arrived), at the pinned copy rates measured here
+    for k, tab in enumerate(tables):
+        want = tab.cpu()
+        for i, (_, _, outs_k, _, _) in enumerate(slots):
+            if not torch.equal(want, outs_k[k]):
+                raise RuntimeError(f"e2e table {k} of slot {i} differs from the device-resident result")
+        if not torch.equal(want, h_out[k]):
+            raise RuntimeError(f"per-call e2e table {k} differs from the device-resident result")
+    for slot in slots:
+        slot[0].close()
+    del slots
+    # the link's bounds at the pinned copy rates measured here: one step alone moves every byte up,
+    # then every byte down (no table can leave before the last triangle has arrived); back-to-back
+    # steps overlap one step's upload with another's read-back, so the slower direction, or both
+    # directions' bytes at the two-way rate, bound them
     rates = copy_rates(torch, 256 << 20)
-    copy_bound_ms = (tris.nbytes / (rates["h2d_gbs"] * 1e9) + 4 * W * 4 / (rates["d2h_gbs"] * 1e9)) * 1e3
+    up_s = tris.nbytes / (rates["h2d_gbs"] * 1e9)
+    down_s = 4 * W * 4 / (rates["d2h_gbs"] * 1e9)
+    both_s = (tris.nbytes + 4 * W * 4) / (rates["both_directions_gbs"] * 1e9)
+    copy_bound_ms = max(up_s, down_s, both_s) * 1e3
+    single_bound_ms = (up_s + down_s) * 1e3
     e2e = {"value": world * 4 * T / (e2e_ms / 1e3) / 1e6, "unit": "Mtris/s", "ms_per_step": e2e_ms,
            "h2d_bytes_per_step": int(tris.nbytes), "d2h_bytes_per_step": int(4 * W * 4),
-           "path": "cvx_plan_create_host, 2 chunks: surface jobs on each chunk as it lands, solid jobs after, "
-                   "each table read back as soon as it is complete",
+           "path": f"{E2E_SLOTS} cvx_plan_create_host plans (own device buffers and host tables) launched on "
+                   f"their own streams in turn, steps back to back; each plan: 2 upload chunks, surface jobs on "
+                   f"each chunk as it lands, solid jobs after, each table read back as soon as it is complete",
+           "l2": f"steps back to back over {E2E_SLOTS} buffer sets ({E2E_SLOTS} x 114 MB of device buffers, "
+                 f"above the 129 MB L2); every step's triangles come up from pinned host memory inside the "
+                 f"timed region",
            "copy_bound_ms": copy_bound_ms, "frac_of_copy_bound": copy_bound_ms / e2e_ms, "copy_rates": rates,
+           "single_step": {"ms_per_step": single_ms, "value": world * 4 * T / (single_ms / 1e3) / 1e6,
+                           "copy_bound_ms": single_bound_ms, "frac_of_copy_bound": single_bound_ms / single_ms,
+                           "note": "one host plan, one step at a time, L2 flushed before each: the round trip's "
+                                   "latency"},
            "plain_calls": {"ms_per_step": plain_e2e_ms, "value": world * 4 * T / (plain_e2e_ms / 1e3) / 1e6,
-                           "note": "upload, 4 calls and 4 read-backs in order on one stream"}}
+                           "note": "upload, 4 calls and 4 read-backs in order on one stream, one step at a "
+                                   "time"}}
 
     # ---- the JSON line; the reference CPU baseline and the side measurements on rank 0 -----------
     extras = {}

@@ -230,7 +230,9 @@ class HostJob:
 class HostPlan:
     """cvx_plan_create_host: the whole round trip -- tables zeroed, triangles up in ``n_chunks``
     pieces (0: the library's default), surface jobs voxelizing each piece as it lands, solid jobs
-    after the last, each table copied down as soon as it is complete -- as one CUDA graph launch."""
+    after the last, each table copied down as soon as it is complete -- as one CUDA graph launch.
+    Plans share no device state: two plans over their own device buffers and host tables, launched
+    on two streams in turn, overlap one round trip's upload with the other's read-back."""
 
     def __init__(self, jobs: Sequence[HostJob], n_chunks: int = 0):
         self._jobs = list(jobs)  # keep buffers alive

@@ -160,7 +160,10 @@ cvx_status cvx_plan_destroy(cvx_plan* plan);
  * d_triangles must share h_triangles and n_triangles (one upload serves them); different uploads
  * and different tables must not overlap.  Host buffers must be page-locked (cudaHostAlloc or
  * cudaHostRegister).  Launch with cvx_plan_launch; the host tables are complete when the launch's
- * stream reaches the point after it.  Destroy with cvx_plan_destroy. */
+ * stream reaches the point after it.  Destroy with cvx_plan_destroy.  Plans share no device state:
+ * host plans over their own device buffers and host tables may be in flight at once on different
+ * streams (one plan's launches run one after another), which overlaps one round trip's upload with
+ * another's read-back. */
 typedef struct cvx_host_job {
 	cvx_voxinfo info;
 	const float* h_triangles; /* host source, n_triangles * 9 floats */

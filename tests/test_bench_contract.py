@@ -37,6 +37,9 @@ def test_engine_arm_prints_one_json_line():
     assert BASE_KEYS | {"roofline", "clocks", "gpu_launches", "tuning"} <= set(line)
     assert line["value"] > 0 and line["gpu_launches"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] > 0 and line["e2e"]["d2h_bytes_per_step"] > 0
+    # back-to-back steps can only beat a lone round trip, and the link bounds both
+    e2e = line["e2e"]
+    assert 0 < e2e["frac_of_copy_bound"] < 1.05 and 0 < e2e["single_step"]["frac_of_copy_bound"] < 1.05
     r = line["roofline"]
     assert {"bound", "achieved", "peak", "unit", "frac", "traffic"} <= set(r)
     assert line["clocks"]["sm_mhz"] is not None

@@ -139,3 +139,31 @@ def test_rejects_pageable_host_memory_and_conflicting_uploads():
     with pytest.raises(cv.CvxError, match="different upload"):
         cv.HostPlan([cv.HostJob(info, pinned, d_tris, torch.zeros(W, dtype=torch.int32).pin_memory(), d_tab),
                      cv.HostJob(info, other, d_tris, torch.zeros(W, dtype=torch.int32).pin_memory(), d_tab2)])
+
+
+def test_two_plans_in_flight_on_two_streams():
+    """Back-to-back steps on two host plans launched on their own streams in turn (the e2e form of
+    the benchmark): each plan owns its counters, queues and flip tables, so the two round trips may
+    overlap and each must still return its own tables exactly.  Different meshes and grids per plan
+    make any shared state show."""
+    slots = []
+    for seed, level, g in ((3, 5, 128), (4, 6, 256)):
+        tris = meshgen.icosphere(seed, level=level)
+        info, jobs = _shared_upload_jobs(tris, g)
+        slots.append((tris, info, jobs, cv.HostPlan(jobs, n_chunks=2), torch.cuda.Stream()))
+    main = torch.cuda.current_stream()
+    start = torch.cuda.Event()
+    start.record(main)
+    for *_, s in slots:
+        s.wait_event(start)
+    for k in range(8):
+        plan, s = slots[k % 2][3:]
+        plan.launch(s)
+    for *_, s in slots:
+        main.wait_stream(s)
+    torch.cuda.synchronize()
+    for tris, info, jobs, plan, _ in slots:
+        for (morton, solid), j in zip(MODES, jobs):
+            want = _alone(info, tris, morton, solid)
+            assert torch.equal(j.h_table, want), f"morton={morton} solid={solid}: {int((j.h_table != want).sum())} words"
+        plan.close()
