@@ -37,9 +37,11 @@ def test_engine_arm_prints_one_json_line():
     assert BASE_KEYS | {"roofline", "clocks", "gpu_launches", "tuning"} <= set(line)
     assert line["value"] > 0 and line["gpu_launches"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] > 0 and line["e2e"]["d2h_bytes_per_step"] > 0
-    # back-to-back steps can only beat a lone round trip, and the link bounds both
+    # the link bounds both forms (the bounds come from copy rates measured beside the steps, so a
+    # fraction a little above 1 is measurement noise; far above would mean bytes were not moved)
     e2e = line["e2e"]
-    assert 0 < e2e["frac_of_copy_bound"] < 1.05 and 0 < e2e["single_step"]["frac_of_copy_bound"] < 1.05
+    assert 0 < e2e["frac_of_copy_bound"] < 1.2 and 0 < e2e["single_step"]["frac_of_copy_bound"] < 1.2
+    assert e2e["ms_per_step"] < e2e["single_step"]["ms_per_step"]
     r = line["roofline"]
     assert {"bound", "achieved", "peak", "unit", "frac", "traffic"} <= set(r)
     assert line["clocks"]["sm_mhz"] is not None
@@ -79,3 +81,16 @@ def test_smoke_resolves_its_imports_without_a_gpu():
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "stopped: smoke() needs cuda:0" in r.stdout
+
+
+def test_link_bound():
+    """Both directions at once while both have bytes left, then the longer one alone; one after the
+    other when running them together is no faster."""
+    sys.path.insert(0, ROOT)
+    import bench
+    r = {"h2d_gbs": 200.0, "d2h_gbs": 200.0, "h2d_with_d2h_gbs": 150.0, "d2h_with_h2d_gbs": 150.0}
+    # 150 MB each way together in 1 ms, then 50 MB down alone in 0.25 ms
+    assert abs(bench.link_bound_s(150e6, 200e6, r) - 1.25e-3) < 1e-12
+    assert abs(bench.link_bound_s(200e6, 150e6, r) - 1.25e-3) < 1e-12
+    slow = dict(r, h2d_with_d2h_gbs=80.0, d2h_with_h2d_gbs=80.0)
+    assert abs(bench.link_bound_s(150e6, 200e6, slow) - 1.75e-3) < 1e-12
