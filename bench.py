@@ -741,37 +741,40 @@ def main():
     # A host-buffer plan (cvx_plan_create_host) is one step's round trip: the triangles go up in 2
     # chunks, the surface jobs voxelize each chunk as it lands, the solid jobs follow, and each table
     # is copied down as soon as it is complete; its graph launch also takes the host's per-call
-    # enqueue time out of the step.  Steps run back to back on E2E_SLOTS such plans, each with its
-    # own device buffers and host tables, launched on their own streams in turn: a step's upload and
-    # kernels run while the step before it is still copying its tables down, so the host link
-    # (about 200 GB/s each way here, 333 GB/s both ways at once) is busy in both directions.  A
-    # third slot measured no faster than two.
-    slots = []
+    # enqueue time out of the step.  Steps run back to back on E2E_SLOTS such plans
+    # (cv.HostPipeline), each with its own device buffers and host tables, launched on their own
+    # streams in turn: a step's upload and kernels run while the step before it is still copying its
+    # tables down, so the host link (about 200 GB/s each way here, 333 GB/s both ways at once) is
+    # busy in both directions.  A third slot measured no faster than two.
+    slot_outs = []
+    slot_jobs = []
     for _ in range(E2E_SLOTS):
         d_k = torch.empty_like(d_tris)
         tabs_k = [torch.empty_like(t) for t in tables]
         outs_k = [torch.empty(W, dtype=torch.int32).pin_memory() for _ in MODES]
-        plan_k = cv.HostPlan([cv.HostJob(info, h_tris, d_k, out, tab, morton, solid)
-                              for (morton, solid), tab, out in zip(MODES, tabs_k, outs_k)], n_chunks=2)
-        slots.append((plan_k, torch.cuda.Stream(), outs_k, d_k, tabs_k))
+        slot_outs.append(outs_k)
+        slot_jobs.append([cv.HostJob(info, h_tris, d_k, out, tab, morton, solid)
+                          for (morton, solid), tab, out in zip(MODES, tabs_k, outs_k)])
+    pipe = cv.HostPipeline(slot_jobs, n_chunks=2)
 
     def e2e_steps(n):
         """n steps back to back, step k on slot k % E2E_SLOTS; returns the events around them."""
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for slot in slots:
-            slot[1].wait_event(a)
-        for k in range(n):
-            plan_k, s = slots[k % E2E_SLOTS][:2]
-            plan_k.launch(s)
-        for slot in slots:
-            stream.wait_stream(slot[1])
+        pipe.begin(stream)
+        for _ in range(n):
+            pipe.submit()
+        pipe.end(stream)
         b.record(stream)
         return a, b
 
+    # a lone round trip: one host plan launched on the timing stream (over slot 0's buffers, never
+    # while the pipeline runs)
+    single = cv.HostPlan(slot_jobs[0], n_chunks=2)
+
     def e2e_step():
-        slots[0][0].launch()
+        single.launch(stream)
 
     def e2e_plain_step():
         d_tris.copy_(h_tris, non_blocking=True)
@@ -813,6 +816,7 @@ def main():
         torch.cuda.synchronize()
         single_times.append(a.elapsed_time(b))
     single_ms = max_over_ranks(float(np.mean(single_times)), world)
+    single.close()
 
     # the timed e2e: K steps back to back over the slots
     e2e_steps(max(3, args.warmup) * E2E_SLOTS)
@@ -829,14 +833,13 @@ def main():
     torch.cuda.synchronize()
     for k, tab in enumerate(tables):
         want = tab.cpu()
-        for i, (_, _, outs_k, _, _) in enumerate(slots):
+        for i, outs_k in enumerate(slot_outs):
             if not torch.equal(want, outs_k[k]):
                 raise RuntimeError(f"e2e table {k} of slot {i} differs from the device-resident result")
         if not torch.equal(want, h_out[k]):
             raise RuntimeError(f"per-call e2e table {k} differs from the device-resident result")
-    for slot in slots:
-        slot[0].close()
-    del slots
+    pipe.close()
+    del pipe, slot_jobs, slot_outs
     # the link's bounds at the pinned copy rates measured here: one step alone moves every byte up,
     # then every byte down (no table can leave before the last triangle has arrived); back-to-back
     # steps can overlap one step's upload with another's read-back, at the rates each direction
@@ -846,17 +849,18 @@ def main():
     single_bound_ms = (tris.nbytes / (rates["h2d_gbs"] * 1e9) + 4 * W * 4 / (rates["d2h_gbs"] * 1e9)) * 1e3
     e2e = {"value": world * 4 * T / (e2e_ms / 1e3) / 1e6, "unit": "Mtris/s", "ms_per_step": e2e_ms,
            "h2d_bytes_per_step": int(tris.nbytes), "d2h_bytes_per_step": int(4 * W * 4),
-           "path": f"{E2E_SLOTS} cvx_plan_create_host plans (own device buffers and host tables) launched on "
-                   f"their own streams in turn, steps back to back; each plan: 2 upload chunks, surface jobs on "
-                   f"each chunk as it lands, solid jobs after, each table read back as soon as it is complete",
+           "path": f"cv.HostPipeline: {E2E_SLOTS} cvx_plan_create_host plans (own device buffers and host "
+                   f"tables) launched on their own streams in turn, steps back to back; each plan: 2 upload "
+                   f"chunks, surface jobs on each chunk as it lands, solid jobs after, each table read back as "
+                   f"soon as it is complete",
            "l2": f"steps back to back over {E2E_SLOTS} buffer sets ({E2E_SLOTS} x 114 MB of device buffers, "
                  f"above the 129 MB L2); every step's triangles come up from pinned host memory inside the "
                  f"timed region",
            "copy_bound_ms": copy_bound_ms, "frac_of_copy_bound": copy_bound_ms / e2e_ms, "copy_rates": rates,
            "single_step": {"ms_per_step": single_ms, "value": world * 4 * T / (single_ms / 1e3) / 1e6,
                            "copy_bound_ms": single_bound_ms, "frac_of_copy_bound": single_bound_ms / single_ms,
-                           "note": "one host plan, one step at a time, L2 flushed before each: the round trip's "
-                                   "latency"},
+                           "note": "one cv.HostPlan launch on the timing stream, one step at a time, L2 flushed "
+                                   "before each: the round trip's latency"},
            "plain_calls": {"ms_per_step": plain_e2e_ms, "value": world * 4 * T / (plain_e2e_ms / 1e3) / 1e6,
                            "note": "upload, 4 calls and 4 read-backs in order on one stream, one step at a "
                                    "time"}}

@@ -275,6 +275,68 @@ class HostPlan:
             pass
 
 
+class HostPipeline:
+    """Round trips back to back: ``len(slots)`` host plans, each over its own device buffers and
+    host tables (``slots[i]`` is slot i's list of HostJob), launched on their own streams in turn,
+    so that one round trip's upload and kernels run while the previous one's tables are still
+    going down.  ``submit()`` launches the next slot and returns its index; that slot's host tables
+    are complete once ``wait(slot)`` returns.  A slot's next launch rewrites its host tables, so
+    read them before the rotation comes back to it (after ``len(slots)`` more submits)."""
+
+    def __init__(self, slots: Sequence[Sequence[HostJob]], n_chunks: int = 0):
+        import torch
+        if not slots:
+            raise ValueError("a pipeline needs at least one slot")
+        # slots run at the same time: no buffer may belong to two of them (jobs of one slot may
+        # share an upload, as in a single host plan)
+        owner = {}
+        for i, s in enumerate(slots):
+            for j in s:
+                for ptr in (_host_ptr(j.h_table, True), _ptr(j.d_table), _ptr(j.d_triangles)):
+                    if ptr and owner.setdefault(ptr, i) != i:
+                        raise ValueError(f"slots {owner[ptr]} and {i} share a buffer: every slot needs its own")
+        self._plans = [HostPlan(s, n_chunks) for s in slots]
+        self._streams = [torch.cuda.Stream() for _ in slots]
+        self._done = [torch.cuda.Event() for _ in slots]
+        self._next = 0
+
+    @property
+    def slots(self) -> int:
+        return len(self._plans)
+
+    def begin(self, stream=None) -> None:
+        """Every slot's next launch follows the work queued so far on `stream` (default: current)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        for st in self._streams:
+            st.wait_stream(s)
+
+    def submit(self) -> int:
+        i = self._next
+        self._plans[i].launch(self._streams[i])
+        self._done[i].record(self._streams[i])
+        self._next = (i + 1) % len(self._plans)
+        return i
+
+    def wait(self, slot: int) -> None:
+        self._done[slot].synchronize()
+
+    def end(self, stream=None) -> None:
+        """Work queued on `stream` (default: current) after this call follows every submitted round trip."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream()
+        for st in self._streams:
+            s.wait_stream(st)
+
+    def kernel_nodes(self) -> int:
+        """Kernel launches of one submit."""
+        return self._plans[0].kernel_nodes()
+
+    def close(self) -> None:
+        for p in getattr(self, "_plans", []):
+            p.close()
+
+
 def profile_enable(on: bool = True) -> None:
     """Record per-kernel CUDA events for the calls of this thread (see profile_collect)."""
     check(lib.cvx_profile_enable(int(bool(on))), "cvx_profile_enable")

@@ -170,3 +170,19 @@ def test_server_stats_struct_layout():
     S = _lib.CvxServerStats
     assert ctypes.sizeof(S) == 136  # static_assert in the library
     assert S.meshes_per_s.offset == 80 and S.queue_p99_ms.offset == 88 and S.issue_p50_us.offset == 128
+
+
+def test_host_pipeline_refuses_slots_sharing_a_buffer():
+    """Slots of a HostPipeline run at the same time, so no device buffer or host table may belong
+    to two of them; the check runs before any plan is built (no GPU call)."""
+    info = _info()
+    h1, h2 = np.zeros(16, np.uint32), np.zeros(16, np.uint32)
+    tri = np.zeros(9, np.float32)
+    a = [cv.HostJob(info, tri, 4096, h1, 8192)]
+    for b in ([cv.HostJob(info, tri, 12288, h1, 16384)],   # the same host table
+              [cv.HostJob(info, tri, 12288, h2, 8192)],    # the same device table
+              [cv.HostJob(info, tri, 4096, h2, 16384)]):   # the same device triangles
+        with pytest.raises(ValueError, match="share a buffer"):
+            cv.HostPipeline([a, b])
+    with pytest.raises(ValueError):
+        cv.HostPipeline([])

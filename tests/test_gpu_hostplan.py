@@ -167,3 +167,30 @@ def test_two_plans_in_flight_on_two_streams():
             want = _alone(info, tris, morton, solid)
             assert torch.equal(j.h_table, want), f"morton={morton} solid={solid}: {int((j.h_table != want).sum())} words"
         plan.close()
+
+
+def test_host_pipeline_slot_results_as_they_complete():
+    """cv.HostPipeline: submit() rotates over the slots; after wait(slot) that slot's host tables
+    hold its round trip's result while the other slots' round trips may still run."""
+    meshes, slot_jobs = [], []
+    for seed, level, g in ((5, 5, 64), (6, 6, 128), (7, 5, 256)):
+        tris = meshgen.icosphere(seed, level=level)
+        info, jobs = _shared_upload_jobs(tris, g)
+        meshes.append((tris, info))
+        slot_jobs.append(jobs)
+    pipe = cv.HostPipeline(slot_jobs, n_chunks=2)
+    assert pipe.slots == 3 and pipe.kernel_nodes() >= 2 * 2 + 3
+    want = [[_alone(info, tris, m, s) for m, s in MODES] for tris, info in meshes]
+    pipe.begin()
+    order = [pipe.submit() for _ in range(3)]
+    assert order == [0, 1, 2]
+    for k in range(9):
+        slot = k % 3
+        pipe.wait(slot)
+        for (morton, solid), j, w in zip(MODES, slot_jobs[slot], want[slot]):
+            assert torch.equal(j.h_table, w), f"slot {slot} morton={morton} solid={solid}"
+            j.h_table.fill_(GARBAGE)  # consumed: the next round trip must write it all again
+        assert pipe.submit() == slot
+    pipe.end()
+    torch.cuda.synchronize()
+    pipe.close()
