@@ -1078,7 +1078,6 @@ def bench_batch(cv, torch, mix, default_tuning=None):
             cv.set_tuning(torch.cuda.current_device(), **default_tuning)
             default_plan_ms = time_plan() * 1e3
             cv.set_tuning(torch.cuda.current_device(), **tuned)
-    plan = cv.Plan(jobs, clear_tables=True)
     # plain: what a caller of the reference drop-in does, one synchronous call per mesh
     def plain():
         for j in jobs:
@@ -1087,7 +1086,6 @@ def bench_batch(cv, torch, mix, default_tuning=None):
             torch.cuda.synchronize()
     plain()
     plain_s = events_s(plain, blocks=3)
-    plan.close()
     return {"batch_256": {"meshes": 256, "triangles": n_tris, "plan_ms": plan_s * 1e3, "plain_ms": plain_s * 1e3,
                           "plan_meshes_s": 256 / plan_s, "plain_meshes_s": 256 / plain_s,
                           "speedup_vs_plain": plain_s / plan_s, "plan_ms_default_tuning": default_plan_ms}}
