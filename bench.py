@@ -872,7 +872,11 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded displaced icosphere)",
             "config": {"workload": "icosphere level 8 (1,310,720 tris) at 512^3; surface+solid x linear+Morton "
                                    "per step", "gridsize": 512, "triangles": T, "l2": "flushed between steps "
-                                   "(512 MiB write, untimed)", "parallelism": f"replicas x{world}"},
+                                   "(512 MiB write, untimed)",
+                       "e2e_l2": f"steps back to back over {E2E_SLOTS} buffer sets ({E2E_SLOTS} x 114 MB of device "
+                                 f"buffers, above the 129 MB L2), every step's triangles copied up from pinned host "
+                                 f"memory inside the timed region; L2 flushed once before the timed steps",
+                       "parallelism": f"replicas x{world}"},
             "clocks": clk.summary(), "gpu_launches": launches_per_step * args.steps, "e2e": e2e, "tuning": tuning,
             "roofline": roofline, "step_per_call": step_calls, "step_sequential": step_seq_line}
 
